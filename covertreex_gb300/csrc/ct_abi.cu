@@ -1,0 +1,158 @@
+// ct_abi.cu — extern "C" entry points of libcovertree_cuda.so (declared in
+// include/covertree_cuda.h).  No torch types cross this boundary: plain device
+// pointers, sizes and a cudaStream_t.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "../../include/covertree_cuda.h"
+#include "ct_common.cuh"
+#include "ct_internal.h"
+#include "ct_tree.h"
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    return fail(CT_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+}  // namespace
+
+#define CT_CUDA(call, where)                          \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+    } while (0)
+
+extern "C" {
+
+int ct_version(void) { return 10000; }
+
+const char* ct_last_error(void) { return g_last_error; }
+
+int ct_build_residual(const float* v, const float* p, const float* coords, int64_t n, int32_t m, int32_t d,
+                      float variance, const float* lengthscale, int32_t n_lengthscale, int32_t kernel_type,
+                      int32_t chunk, int32_t order, uint64_t seed, int32_t flags, void* stream, ct_tree** out) {
+    if (!out) return fail(CT_ERR_ARG, "ct_build_residual: out is NULL");
+    *out = nullptr;
+    if (n <= 0 || n >= (1LL << 31)) return fail(CT_ERR_ARG, "ct_build_residual: n=%lld outside [1, 2^31)", (long long)n);
+    if (m <= 0 || (m % 16) != 0) return fail(CT_ERR_UNSUPPORTED, "ct_build_residual: m=%d must be a positive multiple of 16", m);
+    if (d <= 0 || d > 64) return fail(CT_ERR_ARG, "ct_build_residual: d=%d outside [1, 64]", d);
+    if (!v || !p || !coords) return fail(CT_ERR_ARG, "ct_build_residual: NULL input pointer");
+    if (kernel_type != CT_KERNEL_RBF && kernel_type != CT_KERNEL_MATERN52) kernel_type = CT_KERNEL_RBF;
+    cudaStream_t st = (cudaStream_t)stream;
+
+    ct_tree* T = new (std::nothrow) ct_tree();
+    if (!T) return fail(CT_ERR_NOMEM, "ct_build_residual: host allocation failed");
+    T->n = n; T->m = m; T->d = d; T->var = variance; T->kernel_type = kernel_type;
+    T->chunk = chunk > 0 ? chunk : 512; T->order_mode = order; T->seed = seed;
+
+    // inverse lengthscales exactly as ResidualMetric::new (src/metric.rs:93-101)
+    float inv_ls[64];
+    float fallback = (lengthscale && n_lengthscale > 0) ? lengthscale[0] : 1.0f;
+    for (int i = 0; i < d; ++i) {
+        float raw = (lengthscale && i < n_lengthscale) ? lengthscale[i] : fallback;
+        float safe = fabsf(raw) < 1e-6f ? 1e-6f : raw;
+        inv_ls[i] = 1.0f / safe;
+    }
+    int rc = T->alloc_metric();
+    if (rc != CT_OK) { const char* msg = T->err; int r = fail(rc, "ct_build_residual: %s", msg); delete T; return r; }
+    cudaError_t e = cudaMemcpyAsync(T->inv_ls, inv_ls, sizeof(float) * d, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = ct::launch_metric_setup(v, p, coords, n, m, d, T->inv_ls, T->vperm, T->xs, T->norms, T->p, st);
+    if (e == cudaSuccess && !(flags & CT_BUILD_METRIC_ONLY)) {
+        rc = T->build_tree(v, coords, st);
+        if (rc != CT_OK) { int r = fail(rc, "ct_build_residual: tree build: %s", T->err); delete T; return r; }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "ct_build_residual"); delete T; return r; }
+    *out = T;
+    return CT_OK;
+}
+
+int ct_knn_residual(ct_tree* T, const int64_t* q_ids, int64_t nq, int32_t k, int32_t predecessor, int32_t form,
+                    int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream) {
+    if (!T) return fail(CT_ERR_ARG, "ct_knn_residual: tree is NULL");
+    if (nq < 0) return fail(CT_ERR_ARG, "ct_knn_residual: nq < 0");
+    if (k <= 0) return fail(CT_ERR_ARG, "ct_knn_residual: k=%d must be positive", k);
+    if (k > 128) return fail(CT_ERR_UNSUPPORTED, "ct_knn_residual: k=%d above the supported maximum 128", k);
+    if (nq == 0) return CT_OK;
+    if (!q_ids || !out_idx || !out_dist) return fail(CT_ERR_ARG, "ct_knn_residual: NULL pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    switch (form) {
+        case CT_FORM_DENSE: {
+            int dev = 0;
+            CT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+            int smem_optin = 0;
+            CT_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "smem attr");
+            int qt = ct::brute_pick_qt(T->m, T->d, k, (size_t)smem_optin);
+            if (qt == 0) return fail(CT_ERR_UNSUPPORTED, "ct_knn_residual: m=%d, k=%d exceed shared memory", T->m, k);
+            ct::BruteParams P;
+            P.vperm = T->vperm; P.xs = T->xs; P.norms = T->norms; P.p = T->p;
+            P.qids = (const long long*)q_ids; P.n = T->n; P.nq = nq; P.m = T->m; P.d = T->d; P.k = k;
+            P.kernel_type = T->kernel_type; P.predecessor = predecessor ? 1 : 0; P.var = T->var;
+            P.out_idx = (long long*)out_idx; P.out_dist = out_dist;
+            CT_CUDA(ct::launch_brute_knn(P, qt, st), "dense kNN launch");
+            if (stats) {
+                stats->kernel_launches = 1;
+                stats->distance_evals = predecessor ? 0 : nq * T->n;
+            }
+            return CT_OK;
+        }
+        case CT_FORM_TREE:
+            return T->knn_tree(q_ids, nq, k, predecessor, out_idx, out_dist, stats, st)
+                       ? fail(CT_ERR_STATE, "ct_knn_residual: tree form: %s", T->err)
+                       : CT_OK;
+        case CT_FORM_SCREENED:
+            return T->knn_screened(q_ids, nq, k, predecessor, out_idx, out_dist, stats, st)
+                       ? fail(CT_ERR_STATE, "ct_knn_residual: screened form: %s", T->err)
+                       : CT_OK;
+        default:
+            return fail(CT_ERR_ARG, "ct_knn_residual: unknown form %d", form);
+    }
+}
+
+int ct_tree_arrays(const ct_tree* T, int64_t* parents, int32_t* levels, float* si, int64_t* node_to_dataset,
+                   int64_t* subtree_min, void* stream) {
+    if (!T) return fail(CT_ERR_ARG, "ct_tree_arrays: tree is NULL");
+    if (!T->has_tree) return fail(CT_ERR_STATE, "ct_tree_arrays: tree was built with CT_BUILD_METRIC_ONLY");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)T->n;
+    if (parents) CT_CUDA(cudaMemcpyAsync(parents, T->parents, n * 8, cudaMemcpyDeviceToDevice, st), "copy parents");
+    if (levels) CT_CUDA(cudaMemcpyAsync(levels, T->levels, n * 4, cudaMemcpyDeviceToDevice, st), "copy levels");
+    if (si) CT_CUDA(cudaMemcpyAsync(si, T->si, n * 4, cudaMemcpyDeviceToDevice, st), "copy si");
+    if (node_to_dataset) CT_CUDA(cudaMemcpyAsync(node_to_dataset, T->order, n * 8, cudaMemcpyDeviceToDevice, st), "copy order");
+    if (subtree_min) CT_CUDA(cudaMemcpyAsync(subtree_min, T->sub_min, n * 8, cudaMemcpyDeviceToDevice, st), "copy subtree_min");
+    return CT_OK;
+}
+
+int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {
+    if (!T) return fail(CT_ERR_ARG, "ct_tree_shape: tree is NULL");
+    if (n) *n = T->n;
+    if (m) *m = T->m;
+    if (d) *d = T->d;
+    return CT_OK;
+}
+
+int ct_free(ct_tree* T) {
+    if (!T) return CT_OK;
+    delete T;
+    return CT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,31 @@
+// ct_internal.h — internal declarations shared by the engine's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace ct {
+
+struct BruteParams {
+    const float* vperm;   // n x m, residue-major columns (see ct_setup.cu)
+    const float* xs;      // n x d scaled coordinates
+    const float* norms;   // n squared scaled norms
+    const float* p;       // n residual variances
+    const long long* qids;
+    long long n, nq;
+    int m, d, k, kernel_type, predecessor;
+    float var;
+    long long* out_idx;
+    float* out_dist;
+};
+
+size_t brute_smem_bytes(int qt, int m, int d, int k);
+int brute_pick_qt(int m, int d, int k, size_t smem_limit);
+cudaError_t launch_brute_knn(const BruteParams& P, int qt, cudaStream_t stream);
+
+// ct_setup.cu
+cudaError_t launch_metric_setup(const float* v, const float* p, const float* coords, long long n, int m, int d,
+                                const float* inv_ls_dev, float* vperm, float* xs, float* norms, float* pcopy,
+                                cudaStream_t stream);
+
+}  // namespace ct

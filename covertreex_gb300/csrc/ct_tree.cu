@@ -1,0 +1,36 @@
+// ct_tree.cu — handle memory management; the cover-tree build and traversal
+// live in ct_build.cu and ct_traverse.cu.
+#include "ct_tree.h"
+
+#include "ct_common.cuh"
+
+namespace {
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+}  // namespace
+
+int ct_tree::alloc_metric() {
+    cudaError_t e = dalloc(&vperm, (size_t)n * m);
+    if (e == cudaSuccess) e = dalloc(&xs, (size_t)n * d);
+    if (e == cudaSuccess) e = dalloc(&norms, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&p, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&inv_ls, (size_t)64);
+    if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "device allocation of %lld x %d metric rows failed: %s",
+                                         (long long)n, m, cudaGetErrorString(e));
+    return CT_OK;
+}
+
+ct_tree::~ct_tree() {
+    release_screen();
+    dfree(vperm); dfree(xs); dfree(norms); dfree(p); dfree(inv_ls);
+    dfree(order); dfree(inv); dfree(parents); dfree(levels); dfree(si); dfree(sub_min);
+    dfree(child_off); dfree(child_idx); dfree(roots);
+    dfree(tvperm); dfree(txs); dfree(tnorms); dfree(tp);
+}

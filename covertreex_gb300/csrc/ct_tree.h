@@ -1,0 +1,62 @@
+// ct_tree.h — the opaque ct_tree handle behind the C ABI: device-resident
+// residual metric data, the cover tree, and the buffers of the search forms.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/covertree_cuda.h"
+
+struct ct_tree {
+    // shape and metric parameters
+    int64_t n = 0;
+    int m = 0, d = 0;
+    float var = 1.f;
+    int kernel_type = 0;
+    int chunk = 512, order_mode = CT_ORDER_HILBERT;
+    uint64_t seed = 0;
+
+    // metric data (dataset order), see ct_setup.cu
+    float* vperm = nullptr;
+    float* xs = nullptr;
+    float* norms = nullptr;
+    float* p = nullptr;
+    float* inv_ls = nullptr;
+
+    // cover tree (node order = build order; node i holds dataset row order[i])
+    bool has_tree = false;
+    int64_t* order = nullptr;     // node -> dataset
+    int64_t* inv = nullptr;       // dataset -> node
+    int64_t* parents = nullptr;   // node numbering, -1 for roots
+    int32_t* levels = nullptr;
+    float* si = nullptr;          // cover radius (max distance to any descendant, upper bound)
+    int64_t* sub_min = nullptr;   // min dataset id in the subtree (node itself included)
+    int64_t* child_off = nullptr; // CSR children: child_off[n+1], child_idx[n]
+    int64_t* child_idx = nullptr;
+    int64_t* roots = nullptr;     // root nodes
+    int64_t n_roots = 0;
+    float* tvperm = nullptr;      // tree-order copies for the traversal (residue-major V)
+    float* txs = nullptr;
+    float* tnorms = nullptr;
+    float* tp = nullptr;
+
+    // screened form (BF16 operands, built lazily)
+    void* screen = nullptr;
+
+    char err[256] = "";
+
+    int alloc_metric();
+    int build_tree(const float* v_dataset, const float* coords_dataset, cudaStream_t st);
+    int knn_tree(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
+                 ct_stats* stats, cudaStream_t st);
+    int knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
+                     ct_stats* stats, cudaStream_t st);
+    void release_screen();
+    ~ct_tree();
+
+    template <typename... A>
+    int set_err(int code, const char* fmt, A... a) {
+        snprintf(err, sizeof(err), fmt, a...);
+        return code;
+    }
+};

@@ -1,0 +1,143 @@
+"""Device-side handle: owns a ``ct_tree`` of libcovertree_cuda and its inputs.
+
+PyTorch is used only to hold device memory and to name the CUDA stream; all
+arithmetic happens in the library's own kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+
+
+def _torch():
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("covertreex_gb300 requires a CUDA device (GB300, sm_103a); none is visible")
+    return torch
+
+
+def _stream_ptr(stream) -> ctypes.c_void_p:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(int(s.cuda_stream))
+
+
+def _as_device(a, dtype, device):
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        t = a.to(device=device, dtype=dtype)
+    else:
+        t = torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device=device)
+    return t.contiguous()
+
+
+class CudaResidualIndex:
+    """A residual-correlation metric (and optionally its cover tree) resident on one GPU.
+
+    Mirrors what ``build_pcct2_residual_tree`` returns in the reference
+    (src/lib.rs:1374-1564): the tree handle plus its cached f32 copies.
+    """
+
+    def __init__(self, v_matrix, p_diag, coords, *, variance: float = 1.0, lengthscale=1.0, kernel_type: int = 0,
+                 chunk_size: int = 512, order: str = "hilbert", seed: int = 0, build_tree: bool = True,
+                 device=None, stream=None):
+        torch = _torch()
+        self.device = torch.device(device if device is not None else "cuda")
+        L = _lib.load()
+        v = _as_device(v_matrix, torch.float32, self.device)
+        p = _as_device(p_diag, torch.float32, self.device).reshape(-1)
+        c = _as_device(coords, torch.float32, self.device)
+        if c.dim() == 1:
+            c = c.reshape(-1, 1)
+        if v.dim() != 2 or v.shape[0] != p.shape[0] or c.shape[0] != v.shape[0]:
+            raise ValueError("v_matrix [N,m], p_diag [N] and coords [N,D] must agree on N")
+        self.n, self.m = int(v.shape[0]), int(v.shape[1])
+        self.d = int(c.shape[1])
+        ls = np.atleast_1d(np.asarray(lengthscale, dtype=np.float32))
+        self.lengthscale = ls
+        self.variance = float(variance)
+        self.kernel_type = int(kernel_type)
+        self.has_tree = bool(build_tree)
+        order_code = _lib.CT_ORDER_NATURAL if str(order).lower() == "natural" else _lib.CT_ORDER_HILBERT
+        flags = 0 if build_tree else _lib.CT_BUILD_METRIC_ONLY
+        h = ctypes.c_void_p()
+        ls_c = (ctypes.c_float * ls.size)(*ls.tolist())
+        with torch.cuda.device(self.device):
+            rc = L.ct_build_residual(v.data_ptr(), p.data_ptr(), c.data_ptr(), self.n, self.m, self.d,
+                                     self.variance, ls_c, int(ls.size), self.kernel_type, int(chunk_size),
+                                     order_code, int(seed) & 0xFFFFFFFFFFFFFFFF, flags, _stream_ptr(stream),
+                                     ctypes.byref(h))
+        _lib.check(rc)
+        self._h = h
+        self.last_stats: dict = {}
+
+    # ------------------------------------------------------------------
+    def knn_device(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense", stream=None,
+                   out=None):
+        """Device-in / device-out kNN.  q_ids: int64 CUDA tensor.  Returns (idx, dist) CUDA tensors."""
+        torch = _torch()
+        if self._h is None:
+            raise RuntimeError("index has been freed")
+        k = int(k)
+        if k <= 0:
+            raise ValueError("k must be positive")
+        q = _as_device(q_ids, torch.int64, self.device).reshape(-1)
+        nq = int(q.shape[0])
+        if out is None:
+            idx = torch.empty((nq, k), dtype=torch.int64, device=self.device)
+            dist = torch.empty((nq, k), dtype=torch.float32, device=self.device)
+        else:
+            idx, dist = out
+        st = _lib.CtStats()
+        rc = _lib.load().ct_knn_residual(self._h, q.data_ptr(), nq, k, 1 if predecessor else 0,
+                                         _lib.FORMS[form], idx.data_ptr(), dist.data_ptr(), ctypes.byref(st),
+                                         _stream_ptr(stream))
+        _lib.check(rc)
+        self.last_stats = st.as_dict()
+        return idx, dist
+
+    def knn(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense"):
+        """Host-in / host-out kNN (numpy int64 [Q,k], float32 [Q,k])."""
+        q = np.asarray(q_ids, dtype=np.int64).reshape(-1)
+        if q.size and (q.min() < 0 or q.max() >= self.n):
+            raise ValueError("Residual point decoder received out-of-range indices.")
+        idx, dist = self.knn_device(q, k, predecessor=predecessor, form=form)
+        return idx.cpu().numpy(), dist.cpu().numpy()
+
+    def tree_arrays(self):
+        torch = _torch()
+        if not self.has_tree:
+            raise RuntimeError("index was built without a cover tree")
+        n = self.n
+        parents = torch.empty(n, dtype=torch.int64, device=self.device)
+        levels = torch.empty(n, dtype=torch.int32, device=self.device)
+        si = torch.empty(n, dtype=torch.float32, device=self.device)
+        order = torch.empty(n, dtype=torch.int64, device=self.device)
+        smin = torch.empty(n, dtype=torch.int64, device=self.device)
+        rc = _lib.load().ct_tree_arrays(self._h, parents.data_ptr(), levels.data_ptr(), si.data_ptr(),
+                                        order.data_ptr(), smin.data_ptr(), _stream_ptr(None))
+        _lib.check(rc)
+        torch.cuda.synchronize(self.device)
+        return {"parents": parents.cpu().numpy(), "levels": levels.cpu().numpy(), "si": si.cpu().numpy(),
+                "node_to_dataset": order.cpu().numpy(), "subtree_min": smin.cpu().numpy()}
+
+    def free(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().ct_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def build_vmatrix_cuda(points: np.ndarray, inducing_idx: np.ndarray, *, kernel_type: int, variance: float,
+                       lengthscale: float):
+    raise NotImplementedError("GPU V-matrix construction is not available in this build")

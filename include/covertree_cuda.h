@@ -1,0 +1,123 @@
+/*
+ * covertree_cuda.h — C ABI of libcovertree_cuda.so, the GB300 (sm_103a) engine for
+ * covertreex's residual-correlation cover tree.
+ *
+ * The library replaces the native surface of the reference's PyO3 module
+ * `covertreex_backend` (src/lib.rs:941-952 of covertreex) on the hot path:
+ *   ct_build_residual  <- build_pcct2_residual_tree(v_matrix, p_diag, coords, rbf_var,
+ *                          rbf_ls, chunk_size, batch_order, ..., kernel_type)
+ *                          src/lib.rs:1374-1564
+ *   ct_knn_residual    <- CoverTreeWrapper.knn_query_residual(query_indices, node_to_dataset,
+ *                          v_matrix, p_diag, coords, rbf_var, rbf_ls, k, kernel_type,
+ *                          predecessor_mode, subtree_min_bounds)  src/lib.rs:370-507
+ *                          (output contract of to_py_arrays, src/lib.rs:907-938)
+ *   ct_tree_arrays     <- CoverTreeWrapper.get_parents / get_levels (src/lib.rs:840-900)
+ *                          + compute_subtree_bounds_py (src/lib.rs:991-1006)
+ *   ct_free            <- dropping the CoverTreeWrapper
+ *   ct_last_error      <- the PyErr raised by the bindings (TypeError / RuntimeError)
+ *
+ * Conventions
+ *   - Array arguments are DEVICE pointers unless marked "host".  Row-major, contiguous.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous on that stream except where a comment says otherwise.
+ *   - Every entry point returns CT_OK (0) or a CT_ERR_* code; ct_last_error() gives a
+ *     one-line message for the calling thread's most recent failure.
+ *   - Neighbour output: out_idx int64 [nq x k] dataset ids, out_dist f32 [nq x k],
+ *     ascending by (distance, index); rows with fewer than k neighbours are padded
+ *     with -1 / FLT_MAX (3.402823466e38).
+ */
+#ifndef COVERTREE_CUDA_H
+#define COVERTREE_CUDA_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CT_API __attribute__((visibility("default")))
+#else
+#define CT_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CT_OK 0
+#define CT_ERR_ARG 1
+#define CT_ERR_CUDA 2
+#define CT_ERR_STATE 3
+#define CT_ERR_UNSUPPORTED 4
+#define CT_ERR_TIMEOUT 5
+#define CT_ERR_NOMEM 6
+
+/* kernel_type: the reference's ResidualKernelType (src/metric.rs:44-57). */
+#define CT_KERNEL_RBF 0
+#define CT_KERNEL_MATERN52 1
+
+/* order: batch order of the build (src/lib.rs:1398-1405 batch_order). */
+#define CT_ORDER_NATURAL 0
+#define CT_ORDER_HILBERT 1
+
+/* form: which search ct_knn_residual runs; all return the same neighbour contract. */
+#define CT_FORM_DENSE 0     /* plain FP32, dense sweep, bit-exact reference f32 distances */
+#define CT_FORM_TREE 1      /* plain FP32, cover-tree traversal                          */
+#define CT_FORM_SCREENED 2  /* BF16 tcgen05 screening + compensated rescoring (FP64-grade) */
+
+/* build flags */
+#define CT_BUILD_METRIC_ONLY 1   /* skip the cover-tree build (dense / screened forms only) */
+
+typedef struct ct_tree ct_tree;
+
+typedef struct {
+    int64_t distance_evals;   /* residual distances evaluated (reference `distance_evals`) */
+    int64_t pairs_screened;   /* query x candidate pairs screened by the BF16 pass        */
+    int64_t pairs_rescored;   /* pairs rescored in compensated FP32 / FP64                */
+    int64_t kernel_launches;  /* engine kernels launched by the call                      */
+    double device_ms;         /* device time of the call (0 unless timing was requested)  */
+} ct_stats;
+
+/* Library version (major*10000 + minor*100 + patch). */
+CT_API int ct_version(void);
+
+/* Message of the calling thread's last failure ("" if none). */
+CT_API const char* ct_last_error(void);
+
+/*
+ * Build the device-resident residual metric and cover tree.
+ *   v [n x m], p [n], coords [n x d]: device, f32 (the reference casts to f32 too).
+ *   lengthscale: HOST pointer to n_lengthscale floats (missing axes reuse entry 0,
+ *   |l| < 1e-6 is clamped to 1e-6, src/metric.rs:93-101).
+ *   variance: kernel variance (rbf_var).  kernel_type: CT_KERNEL_*.
+ *   chunk: batch-insert chunk size (reference default 512).  order: CT_ORDER_*.
+ *   seed: MIS seed.  flags: CT_BUILD_*.
+ * The inputs are copied; the caller may free them after the call returns.
+ * Synchronises `stream` once at the end of the build.
+ */
+CT_API int ct_build_residual(const float* v, const float* p, const float* coords, int64_t n, int32_t m, int32_t d,
+                      float variance, const float* lengthscale, int32_t n_lengthscale, int32_t kernel_type,
+                      int32_t chunk, int32_t order, uint64_t seed, int32_t flags, void* stream, ct_tree** out);
+
+/*
+ * k nearest neighbours of dataset rows q_ids[0..nq) (device int64).
+ *   predecessor != 0: only neighbours j < q_id (Vecchia ordering).
+ *   Ids outside [0, n) produce an all-padding row.
+ *   stats may be NULL.
+ */
+CT_API int ct_knn_residual(ct_tree* tree, const int64_t* q_ids, int64_t nq, int32_t k, int32_t predecessor, int32_t form,
+                    int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream);
+
+/* Copy tree arrays to device buffers of n entries each (any may be NULL):
+ * parents (node numbering), levels, si (cover radii), node_to_dataset, subtree_min. */
+CT_API int ct_tree_arrays(const ct_tree* tree, int64_t* parents, int32_t* levels, float* si, int64_t* node_to_dataset,
+                   int64_t* subtree_min, void* stream);
+
+/* n, m, d of a tree (host outputs; any may be NULL). */
+CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
+
+/* Release a tree and its device memory. */
+CT_API int ct_free(ct_tree* tree);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COVERTREE_CUDA_H */

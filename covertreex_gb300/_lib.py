@@ -39,6 +39,7 @@ EXPORTED_SYMBOLS = (
     "ct_knn_residual",
     "ct_tree_arrays",
     "ct_tree_shape",
+    "ct_debug_screen_dots",
     "ct_free",
 )
 
@@ -97,6 +98,8 @@ def load(build_if_missing: bool = True):
         L.ct_tree_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.ct_tree_shape.restype = ctypes.c_int
         L.ct_tree_shape.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i32), ctypes.POINTER(i32)]
+        L.ct_debug_screen_dots.restype = ctypes.c_int
+        L.ct_debug_screen_dots.argtypes = [vp, vp, vp, vp, vp]
         L.ct_free.restype = ctypes.c_int
         L.ct_free.argtypes = [vp]
         _handle = L

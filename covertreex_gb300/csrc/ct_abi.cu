@@ -14,6 +14,8 @@
 #include "ct_internal.h"
 #include "ct_tree.h"
 
+int ct_screen_debug_dots(ct_tree* T, const int* rows_a, const int* rows_b, float* out, cudaStream_t st);
+
 namespace {
 
 thread_local char g_last_error[512] = "";
@@ -68,10 +70,13 @@ int ct_build_residual(const float* v, const float* p, const float* coords, int64
         float raw = (lengthscale && i < n_lengthscale) ? lengthscale[i] : fallback;
         float safe = fabsf(raw) < 1e-6f ? 1e-6f : raw;
         inv_ls[i] = 1.0f / safe;
+        T->inv_ls_host64[i] = 1.0 / (double)safe;
     }
     int rc = T->alloc_metric();
     if (rc != CT_OK) { const char* msg = T->err; int r = fail(rc, "ct_build_residual: %s", msg); delete T; return r; }
     cudaError_t e = cudaMemcpyAsync(T->inv_ls, inv_ls, sizeof(float) * d, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->vnat, v, sizeof(float) * (size_t)n * m, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(T->coords_raw, coords, sizeof(float) * (size_t)n * d, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess)
         e = ct::launch_metric_setup(v, p, coords, n, m, d, T->inv_ls, T->vperm, T->xs, T->norms, T->p, st);
     if (e == cudaSuccess && !(flags & CT_BUILD_METRIC_ONLY)) {
@@ -139,6 +144,12 @@ int ct_tree_arrays(const ct_tree* T, int64_t* parents, int32_t* levels, float* s
     if (node_to_dataset) CT_CUDA(cudaMemcpyAsync(node_to_dataset, T->order, n * 8, cudaMemcpyDeviceToDevice, st), "copy order");
     if (subtree_min) CT_CUDA(cudaMemcpyAsync(subtree_min, T->sub_min, n * 8, cudaMemcpyDeviceToDevice, st), "copy subtree_min");
     return CT_OK;
+}
+
+int ct_debug_screen_dots(ct_tree* T, const int32_t* rows_a, const int32_t* rows_b, float* out, void* stream) {
+    if (!T || !rows_a || !rows_b || !out) return fail(CT_ERR_ARG, "ct_debug_screen_dots: NULL argument");
+    int rc = ct_screen_debug_dots(T, rows_a, rows_b, out, (cudaStream_t)stream);
+    return rc ? fail(rc, "ct_debug_screen_dots: %s", T->err) : CT_OK;
 }
 
 int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {

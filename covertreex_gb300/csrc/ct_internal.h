@@ -28,4 +28,11 @@ cudaError_t launch_metric_setup(const float* v, const float* p, const float* coo
                                 const float* inv_ls_dev, float* vperm, float* xs, float* norms, float* pcopy,
                                 cudaStream_t stream);
 
+// ct_order.cu
+cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st);
+cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long long* ktmp, int* vtmp, long long n,
+                             int kbits, unsigned* hist, void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st,
+                             bool* result_in_tmp);
+int radix_num_blocks(long long n);
+
 }  // namespace ct

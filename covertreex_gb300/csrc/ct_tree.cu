@@ -22,6 +22,8 @@ int ct_tree::alloc_metric() {
     if (e == cudaSuccess) e = dalloc(&norms, (size_t)n);
     if (e == cudaSuccess) e = dalloc(&p, (size_t)n);
     if (e == cudaSuccess) e = dalloc(&inv_ls, (size_t)64);
+    if (e == cudaSuccess) e = dalloc(&vnat, (size_t)n * m);
+    if (e == cudaSuccess) e = dalloc(&coords_raw, (size_t)n * d);
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "device allocation of %lld x %d metric rows failed: %s",
                                          (long long)n, m, cudaGetErrorString(e));
     return CT_OK;
@@ -29,7 +31,7 @@ int ct_tree::alloc_metric() {
 
 ct_tree::~ct_tree() {
     release_screen();
-    dfree(vperm); dfree(xs); dfree(norms); dfree(p); dfree(inv_ls);
+    dfree(vperm); dfree(xs); dfree(norms); dfree(p); dfree(inv_ls); dfree(vnat); dfree(coords_raw);
     dfree(order); dfree(inv); dfree(parents); dfree(levels); dfree(si); dfree(sub_min);
     dfree(child_off); dfree(child_idx); dfree(roots);
     dfree(tvperm); dfree(txs); dfree(tnorms); dfree(tp);

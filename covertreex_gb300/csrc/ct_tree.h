@@ -22,6 +22,9 @@ struct ct_tree {
     float* norms = nullptr;
     float* p = nullptr;
     float* inv_ls = nullptr;
+    float* vnat = nullptr;        // V in natural layout (dataset order), for operand prep / rescoring
+    float* coords_raw = nullptr;  // unscaled coordinates (dataset order)
+    double inv_ls_host64[64] = {0};
 
     // cover tree (node order = build order; node i holds dataset row order[i])
     bool has_tree = false;

@@ -109,6 +109,20 @@ class CudaResidualIndex:
         idx, dist = self.knn_device(q, k, predecessor=predecessor, form=form)
         return idx.cpu().numpy(), dist.cpu().numpy()
 
+    def debug_screen_dots(self, rows_a, rows_b):
+        """Raw BF16-screened dot products (hi.hi + hi.lo + lo.hi) of 128 x 256 dataset rows."""
+        torch = _torch()
+        ra = torch.full((128,), -1, dtype=torch.int32, device=self.device)
+        rb = torch.full((256,), -1, dtype=torch.int32, device=self.device)
+        a = torch.as_tensor(np.asarray(rows_a, dtype=np.int32))
+        b = torch.as_tensor(np.asarray(rows_b, dtype=np.int32))
+        ra[: a.numel()] = a.to(self.device)
+        rb[: b.numel()] = b.to(self.device)
+        out = torch.empty((128, 256), dtype=torch.float32, device=self.device)
+        rc = _lib.load().ct_debug_screen_dots(self._h, ra.data_ptr(), rb.data_ptr(), out.data_ptr(), _stream_ptr(None))
+        _lib.check(rc)
+        return out.cpu().numpy()
+
     def tree_arrays(self):
         torch = _torch()
         if not self.has_tree:

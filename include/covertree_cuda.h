@@ -110,6 +110,14 @@ CT_API int ct_knn_residual(ct_tree* tree, const int64_t* q_ids, int64_t nq, int3
 CT_API int ct_tree_arrays(const ct_tree* tree, int64_t* parents, int32_t* levels, float* si, int64_t* node_to_dataset,
                    int64_t* subtree_min, void* stream);
 
+/* Diagnostic: the BF16 screening pass's raw FP32 dot products hi.hi + hi.lo + lo.hi for
+ * the 128 x 256 block rows_a (128 device int32 dataset rows, -1 = zero row) x rows_b
+ * (256 device int32 rows) into out (device f32 [128 x 256], row-major).  No counterpart
+ * in the reference; exposed so the tensor-core path can be checked against FP64.
+ * Synchronises `stream`. */
+CT_API int ct_debug_screen_dots(ct_tree* tree, const int32_t* rows_a, const int32_t* rows_b, float* out,
+                                void* stream);
+
 /* n, m, d of a tree (host outputs; any may be NULL). */
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
 

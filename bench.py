@@ -1,0 +1,366 @@
+#!/usr/bin/env python3
+"""Benchmark of the residual-correlation kNN hot path on one GB300 (or N, sharded).
+
+Metric: residual kNN queries/s (and p99 step latency), BF16-screened form vs the
+plain FP32 form, same neighbours.  Default workload = the precision-form shape:
+N=262144, D=8, m=512, k=50, predecessor_mode=True, Q = all N queries, RBF l=2 over
+a seeded mixture of 16 Gaussians (synthetic; no dataset exists for it).
+
+One step = one ct_knn_residual call over the whole query set with V, coords and
+queries resident in HBM.  `e2e` repeats the step through the host-facing call:
+query ids copied from pinned host memory, results copied back to pinned host
+memory, all inside the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) each rank holds a replica of the metric and takes an
+interleaved slice of the queries (no data-path collective); the max over ranks
+of the timed region gives the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "residual kNN queries/s & p99 ms, BF16-screened vs plain FP32 GPU, same neighbours"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["precision", "readme", "plain_small"], default="precision")
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP32 form (0 = skip)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=2048, help="queries per CPU baseline sample")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, backend):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def shard_queries(nq: int, world: int, rank: int) -> np.ndarray:
+    """Interleaved slice: balances the triangular cost of predecessor mode across ranks."""
+    return np.arange(rank, nq, world, dtype=np.int64)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU (oracle) legs
+def oracle_queries_per_s(wl, sample: int, threads: int, parity: bool, seed: int = 4, tree=None):
+    """Time the restated rust-hilbert engine (oracle/ct_oracle.c) on `sample` random queries."""
+    from oracle import oracle as O
+
+    if tree is None:
+        t0 = time.perf_counter()
+        tree = O.OracleResidualTree(wl.v, wl.p, wl.coords, wl.variance, [wl.lengthscale] * wl.d,
+                                    kernel_type=wl.kernel_type, chunk=512, order="hilbert", parity=parity)
+        tree.build_seconds = time.perf_counter() - t0
+    q = np.random.default_rng(seed).choice(wl.n, min(sample, wl.n), replace=False)
+    t0 = time.perf_counter()
+    tree.knn(q, wl.k, predecessor=wl.predecessor, parity=parity, threads=threads)
+    dt = time.perf_counter() - t0
+    return q.size / dt, tree
+
+
+def run_reference(args, wl):
+    """--impl reference: the reference's own CPU algorithm (restated rust-hilbert, default
+    budget mode) on this machine's host cores; each step is a bounded query sample."""
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    qps, tree = oracle_queries_per_s(wl, 64, threads, parity=False)
+    build_s = tree.build_seconds
+    for w in range(args.warmup):
+        oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False, seed=100 + w, tree=tree)
+    times = []
+    for s in range(args.steps):
+        q = np.random.default_rng(200 + s).choice(wl.n, min(args.cpu_sample, wl.n), replace=False)
+        t1 = time.perf_counter()
+        tree.knn(q, wl.k, predecessor=wl.predecessor, parity=False, threads=threads)
+        times.append(time.perf_counter() - t1)
+    ms = float(np.mean(times) * 1e3)
+    value = args.cpu_sample / (ms / 1e3)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "p99_ms": float(np.percentile(np.array(times) * 1e3, 99)), "higher_is_better": True, "scaling": "strong",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": wl.describe(), "engine": "rust-hilbert restated in C (oracle/ct_oracle.c), default budget mode"},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.cpu_sample} random query ids per step; tree build {build_s:.2f} s excluded"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "build_seconds": build_s,
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU leg
+def main():
+    args = parse_args()
+    world, rank, local = dist_env()
+    from covertreex_gb300 import synthetic
+
+    if args.impl == "reference":
+        if rank == 0:
+            import subprocess as sp
+
+            sp.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+            wl = synthetic.make(args.workload)
+            run_reference(args, wl)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = dist_init(world, "nccl")
+    from covertreex_gb300 import _build, _lib
+    from covertreex_gb300.device import CudaResidualIndex
+
+    _build.build_library()
+    L = _lib.load()
+    wl = synthetic.make(args.workload)
+    dev = torch.device("cuda", local)
+    index = CudaResidualIndex(wl.v, wl.p, wl.coords, variance=wl.variance, lengthscale=[wl.lengthscale] * wl.d,
+                              kernel_type=wl.kernel_type, build_tree=False, device=dev)
+    q_host = shard_queries(wl.n, world, rank)
+    q_dev = torch.as_tensor(q_host, device=dev)
+    nq = int(q_dev.numel())
+    idx_out = torch.empty((nq, wl.k), dtype=torch.int64, device=dev)
+    dist_out = torch.empty((nq, wl.k), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(form):
+        index.knn_device(q_dev, wl.k, predecessor=wl.predecessor, form=form, out=(idx_out, dist_out))
+        return index.last_stats
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x: float) -> float:
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- warm-up (screened form builds its operands lazily on first use)
+    L.ct_set_timing(1)
+    for _ in range(max(args.warmup, 3)):
+        step("screened")
+    # ---- timed region (screened)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stats = []
+    t_wall0 = time.perf_counter()
+    for s in range(args.steps):
+        ev[s][0].record(stream)
+        stats.append(dict(step("screened")))
+        ev[s][1].record(stream)
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = sampler.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = max_over_ranks(float(np.sum(step_ms)))
+    ms_per_step = total_ms / args.steps
+    q_total = wl.n  # all ranks together process every query once per step
+    value = q_total / (ms_per_step / 1e3)
+    screened_idx = idx_out.clone()
+    screened_dist = dist_out.clone()
+
+    # ---- e2e through the host-facing call (pinned host buffers, copies timed)
+    q_pin = torch.as_tensor(q_host).pin_memory()
+    idx_pin = torch.empty((nq, wl.k), dtype=torch.int64).pin_memory()
+    dist_pin = torch.empty((nq, wl.k), dtype=torch.float32).pin_memory()
+    barrier()
+    e2e_ms = []
+    for s in range(args.steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        qd = q_pin.to(dev, non_blocking=True)
+        i_d, d_d = index.knn_device(qd, wl.k, predecessor=wl.predecessor, form="screened")
+        idx_pin.copy_(i_d, non_blocking=True)
+        dist_pin.copy_(d_d, non_blocking=True)
+        b.record(stream)
+        b.synchronize()
+        e2e_ms.append(a.elapsed_time(b))
+    e2e_total = max_over_ranks(float(np.sum(e2e_ms)))
+    e2e_value = q_total / (e2e_total / args.steps / 1e3)
+
+    # ---- plain FP32 form (dense sweep, bit-exact reference f32 distances)
+    plain = None
+    agree = None
+    if args.plain_steps > 0:
+        step("dense")
+        barrier()
+        pm = []
+        for _ in range(args.plain_steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step("dense")
+            b.record(stream)
+            b.synchronize()
+            pm.append(a.elapsed_time(b))
+        p_ms = max_over_ranks(float(np.mean(pm)))
+        plain = {"value": q_total / (p_ms / 1e3), "unit": "queries/s", "ms_per_step": p_ms, "steps": args.plain_steps,
+                 "dtype": "f32"}
+        si = screened_idx.cpu().numpy()
+        di = idx_out.cpu().numpy()
+        same = np.all(np.sort(si, axis=1) == np.sort(di, axis=1), axis=1)
+        pv = torch.as_tensor(wl.p)[torch.as_tensor(q_host)].numpy()
+        well = pv >= 0.05
+        agree = {"all_rows": float(same.mean()), "rows_p_ge_0.05": float(same[well].mean()) if well.any() else None}
+
+    # ---- roofline of the dominant kernel (Pass B tensor-core screening)
+    hbm, bf16_burst, bf16_sus, peak_kind = measured_peaks()
+    st = stats[-1]
+    pairs_main = st["screen_pairs_main"]
+    screen_ms = float(np.mean([s["screen_ms"] for s in stats]))
+    alg_flops = 2.0 * wl.m * pairs_main             # per-unit figure 2m flops per screened pair
+    issued_flops = 3.0 * alg_flops                  # hi.hi + hi.lo + lo.hi
+    achieved = alg_flops / (screen_ms / 1e3) / 1e12
+    roofline = {
+        "bound": "tensor", "kernel": "screen_mma_kernel (main sweep)", "achieved": achieved,
+        "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus, "traffic": None,
+        "peak_kind": f"bf16_tflops_sustained ({peak_kind})",
+        "tensor_issued_tflops": issued_flops / (screen_ms / 1e3) / 1e12,
+        "kernel_ms": screen_ms, "pairs_per_launch": pairs_main,
+        "phase_ms": {"threshold": float(np.mean([s["threshold_ms"] for s in stats])), "screen": screen_ms,
+                     "rescore": float(np.mean([s["rescore_ms"] for s in stats])),
+                     "call": float(np.mean([s["device_ms"] for s in stats]))},
+    }
+
+    # ---- CPU baseline (rank 0, N=1 only): restated rust-hilbert on host cores
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+            threads = os.cpu_count() or 1
+            qps, tree = oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False)
+            cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                   "sample": f"{min(args.cpu_sample, wl.n)} random query ids of the same workload, default budget "
+                             f"mode; tree build {tree.build_seconds:.2f} s excluded"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"unavailable: {exc}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "p99_ms": float(np.percentile(step_ms, 99)), "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded; no public dataset for this shape)",
+            "config": {"workload": wl.describe(), "form": "screened", "N": wl.n, "D": wl.d, "m": wl.m, "k": wl.k,
+                       "predecessor": wl.predecessor, "queries": wl.n, "parallelism": f"query-shard x{world}",
+                       "l2": "inputs larger than L2 (V f32 512 MiB + bf16 hi/lo blocks 1 GiB)"},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q_pin.numel() * 8),
+                    "d2h_bytes_per_step": int(nq * wl.k * 12)},
+            "clocks": clocks,
+            "gpu_launches": int(sum(s["kernel_launches"] for s in stats)),
+            "plain_fp32": plain,
+            "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,
+            "neighbour_agreement_vs_plain": agree,
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

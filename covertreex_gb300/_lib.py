@@ -34,6 +34,7 @@ FORMS = {"dense": CT_FORM_DENSE, "tree": CT_FORM_TREE, "screened": CT_FORM_SCREE
 #: every symbol include/covertree_cuda.h declares
 EXPORTED_SYMBOLS = (
     "ct_version",
+    "ct_set_timing",
     "ct_last_error",
     "ct_build_residual",
     "ct_knn_residual",
@@ -51,6 +52,11 @@ class CtStats(ctypes.Structure):
         ("pairs_rescored", ctypes.c_int64),
         ("kernel_launches", ctypes.c_int64),
         ("device_ms", ctypes.c_double),
+        ("screen_ms", ctypes.c_double),
+        ("threshold_ms", ctypes.c_double),
+        ("rescore_ms", ctypes.c_double),
+        ("screen_pairs_main", ctypes.c_int64),
+        ("overflow_queries", ctypes.c_int64),
     ]
 
     def as_dict(self):
@@ -87,6 +93,8 @@ def load(build_if_missing: bool = True):
         i64, i32, f32, u64 = ctypes.c_int64, ctypes.c_int32, ctypes.c_float, ctypes.c_uint64
         L.ct_version.restype = ctypes.c_int
         L.ct_version.argtypes = []
+        L.ct_set_timing.restype = ctypes.c_int
+        L.ct_set_timing.argtypes = [ctypes.c_int]
         L.ct_last_error.restype = ctypes.c_char_p
         L.ct_last_error.argtypes = []
         L.ct_build_residual.restype = ctypes.c_int

@@ -19,6 +19,7 @@ int ct_screen_debug_dots(ct_tree* T, const int* rows_a, const int* rows_b, float
 namespace {
 
 thread_local char g_last_error[512] = "";
+thread_local bool g_timing = false;
 
 int fail(int code, const char* fmt, ...) {
     va_list ap;
@@ -34,6 +35,10 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 }  // namespace
 
+namespace ct {
+bool timing_enabled() { return g_timing; }
+}  // namespace ct
+
 #define CT_CUDA(call, where)                          \
     do {                                              \
         cudaError_t e_ = (call);                      \
@@ -43,6 +48,11 @@ int cuda_fail(cudaError_t e, const char* where) {
 extern "C" {
 
 int ct_version(void) { return 10000; }
+
+int ct_set_timing(int enable) {
+    g_timing = enable != 0;
+    return CT_OK;
+}
 
 const char* ct_last_error(void) { return g_last_error; }
 
@@ -112,10 +122,24 @@ int ct_knn_residual(ct_tree* T, const int64_t* q_ids, int64_t nq, int32_t k, int
             P.qids = (const long long*)q_ids; P.n = T->n; P.nq = nq; P.m = T->m; P.d = T->d; P.k = k;
             P.kernel_type = T->kernel_type; P.predecessor = predecessor ? 1 : 0; P.var = T->var;
             P.out_idx = (long long*)out_idx; P.out_dist = out_dist;
+            cudaEvent_t e0 = nullptr, e1 = nullptr;
+            if (g_timing) {
+                CT_CUDA(cudaEventCreate(&e0), "event");
+                CT_CUDA(cudaEventCreate(&e1), "event");
+                CT_CUDA(cudaEventRecord(e0, st), "event record");
+            }
             CT_CUDA(ct::launch_brute_knn(P, qt, st), "dense kNN launch");
+            if (g_timing) {
+                float ms = 0.f;
+                CT_CUDA(cudaEventRecord(e1, st), "event record");
+                CT_CUDA(cudaEventSynchronize(e1), "event sync");
+                CT_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event time");
+                cudaEventDestroy(e0); cudaEventDestroy(e1);
+                if (stats) { stats->device_ms = ms; stats->screen_ms = ms; }
+            }
             if (stats) {
                 stats->kernel_launches = 1;
-                stats->distance_evals = predecessor ? 0 : nq * T->n;
+                stats->distance_evals = predecessor ? -1 : nq * T->n;
             }
             return CT_OK;
         }

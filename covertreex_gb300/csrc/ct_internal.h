@@ -6,6 +6,9 @@
 
 namespace ct {
 
+// per-thread timing switch (ct_set_timing)
+bool timing_enabled();
+
 struct BruteParams {
     const float* vperm;   // n x m, residue-major columns (see ct_setup.cu)
     const float* xs;      // n x d scaled coordinates
@@ -29,7 +32,8 @@ cudaError_t launch_metric_setup(const float* v, const float* p, const float* coo
                                 cudaStream_t stream);
 
 // ct_order.cu
-cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st);
+cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st,
+                          unsigned long long* keys_by_id = nullptr);
 cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long long* ktmp, int* vtmp, long long n,
                              int kbits, unsigned* hist, void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st,
                              bool* result_in_tmp);

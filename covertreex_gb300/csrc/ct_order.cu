@@ -248,7 +248,8 @@ int radix_num_blocks(long long n) { return (int)((n + kTile - 1) / kTile); }
 
 // Compute the batch order of `coords` (n x d, f32): order[i] = dataset row of
 // sorted position i.  mode 1 = Hilbert (D-generic), 2 = Morton (D == 3 only).
-cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st) {
+cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st,
+                          unsigned long long* keys_by_id) {
     if (n <= 0) return cudaSuccess;
     double* mm = nullptr;
     unsigned long long *keys = nullptr, *ktmp = nullptr;
@@ -282,6 +283,8 @@ cudaError_t compute_order(const float* coords, long long n, int d, int mode, int
             kbits = bits * d;
         }
         e = cudaGetLastError();
+        if (e == cudaSuccess && keys_by_id)
+            e = cudaMemcpyAsync(keys_by_id, keys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, st);
         bool in_tmp = false;
         if (e == cudaSuccess) e = radix_sort_pairs(keys, order_out, ktmp, vtmp, n, kbits, hist, scan, scan_bytes, st, &in_tmp);
         if (e == cudaSuccess && in_tmp) e = cudaMemcpyAsync(order_out, vtmp, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);

@@ -5,21 +5,24 @@
 //   1. Operands.  V is split as v = hi + lo (hi = bf16(v), lo = bf16(v - hi)) and
 //      stored in the UMMA "blocked" layout: for each K-chunk of 32 columns and
 //      each group of 8 rows, one 512-byte block of four 8x8 core matrices.  A
-//      K-chunk of a 128- or 256-row tile is therefore one contiguous span that a
-//      single 1-D bulk copy (TMA) moves into shared memory.
-//   2. Pass A (threshold).  Query tiles in Hilbert order meet the W candidate
-//      tiles around them in Hilbert order.  s = hi.hi + hi.lo + lo.hi is
-//      accumulated in TMEM by tcgen05.mma (kind::f16, M=128, N=256, K=16); the
-//      epilogue turns s into a certified upper bound of each squared residual
-//      distance, and tau_q^2 is the k-th smallest bound among valid candidates,
-//      an upper bound of the true k-th distance.
-//   3. Pass B (screen).  Query tiles in dataset order sweep the candidate tiles
-//      (the lower triangle in predecessor mode); every candidate whose certified
-//      lower bound is <= tau_q^2 is appended to the query's survivor list.
-//   4. Rescore.  Each survivor's distance is recomputed from the f32 inputs with
+//      K-chunk of a 128- or 256-row tile is one contiguous span that a single
+//      1-D bulk copy (TMA) moves into shared memory.
+//   2. Sweep.  A CTA owns a tile of 128 queries (sorted by Hilbert position
+//      inside their "level": the dataset prefix [0, 2^j) with 2^j <= q in
+//      predecessor mode, the whole dataset otherwise) and sweeps its candidate
+//      tiles nearest-first: the level's Hilbert tiles in a spiral around the
+//      queries, then (predecessor mode) the dataset tiles [2^j, max q).  For every
+//      query x candidate pair, s = hi.hi + hi.lo + lo.hi is accumulated in TMEM
+//      by tcgen05.mma (kind::f16, M=128, N=256, K=16) and the epilogue turns it
+//      into certified bounds [dl2, du2] of the squared residual distance.  Each
+//      epilogue thread keeps the k smallest du2 of its row half in a heap; the
+//      k-th is an upper bound tau^2 of the true k-th distance, and every
+//      candidate with dl2 <= tau^2 (tau as it stands when the pair is seen) is
+//      kept.  Spiral order makes tau tight after the first tiles.
+//   3. Rescore.  Each survivor's distance is recomputed from the f32 inputs with
 //      a compensated FP32 dot product (TwoProd/TwoSum) and an FP64 kernel value
 //      and normalisation; the k best (distance, index) pairs are written out.
-//      Queries whose list overflowed are rescored against every valid candidate.
+//      Queries whose survivor list overflowed are rescored exhaustively.
 //
 // Error bound of the screened dot (per pair), with u = 2^-8 (bf16) and
 // v = hi + lo + r, |r| <= u^2 |v|:  |s - v_q.v_c| <= c_split ||v_q|| ||v_c|| with
@@ -28,6 +31,7 @@
 // step's internal alignment), both relative to sum |v_qi v_ci| <= ||v_q|| ||v_c||.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -45,18 +49,21 @@ namespace sm = ct::sm100;
 constexpr int TQ = 128;
 constexpr int TC = 256;
 constexpr int KC = 32;
-constexpr int STAGES = 3;
+constexpr int STAGES = 3;  // maximum; the launch picks 3 or 2 to fit the heaps
 constexpr int CHUNK_A = TQ * KC * 2;  // bytes
 constexpr int CHUNK_B = TC * KC * 2;
 constexpr int STAGE_BYTES = 2 * CHUNK_A + 2 * CHUNK_B;
 constexpr int kEpiWarps = 8;
-constexpr int kThreads = 64 + 32 * kEpiWarps;
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kThreads = 96 + kEpiThreads;  // producer, MMA issuer, staging, epilogue
 constexpr int kMaxD = 8;
-constexpr int WINDOW_TILES = 4;
+constexpr int kMaxK = 64;                   // heap capacity per epilogue thread
+constexpr int REC = 12;                     // floats per staged candidate record
 constexpr int SURV_CAP = 1024;
-constexpr int RBUF = 1024;  // rescoring sort buffer (power of two)
+constexpr int HALF_CAP = SURV_CAP / 2;  // survivor segment per (query, column half)
+constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
 
-enum Mode { MODE_DEBUG = 0, MODE_WINDOW = 1, MODE_FILTER = 2 };
+enum Mode { MODE_DEBUG = 0, MODE_SWEEP = 1 };
 
 // element offset of (row, col) in a blocked matrix with G = rows_pad / 8 row groups
 __host__ __device__ inline size_t blocked_offset(long long row, int col, long long G) {
@@ -66,103 +73,114 @@ __host__ __device__ inline size_t blocked_offset(long long row, int col, long lo
     return ((size_t)c * (size_t)G + (size_t)g) * 256 + (size_t)j * 64 + (size_t)rr * 8 + e;
 }
 
+// One job = one candidate tile for the CTA's current query tile.
 struct Job {
-    int qtile, ctile, slot, pad;
+    int qtile;  // query tile (rows qtile*128 .. of the A operand)
+    int ctile;  // candidate tile in the B matrix selected by `which`
+    int which;  // bit 0: 0 = level matrix (Hilbert order), 1 = dataset matrix;
+                // bit 1: warm-up job (bounds feed the thresholds, nothing is kept);
+                // bit 2: kept job whose tile already fed the thresholds in warm-up
+    int first;  // 1 on the first job of a query tile
 };
 
 struct MMAParams {
     const bf16* a_hi; const bf16* a_lo; long long a_groups;
-    const bf16* b_hi; const bf16* b_lo; long long b_groups;
+    const bf16* b_hi[2]; const bf16* b_lo[2]; long long b_groups[2];
+    const int* b_id[2];  // B row -> dataset id (or -1)
     int m;
-    const Job* jobs; int njobs;
+    const Job* jobs;
+    const int* cta_job_begin;  // per CTA: [begin, end) into jobs
     const int* a_slot;   // A row -> query slot (or -1)
     const int* slot_id;  // query slot -> dataset id
-    const int* b_id;     // B row -> dataset id (or -1)
     const float* xs; int d;
     const float* vn; const float* isp; const float* xmax;
     float var; int kernel_type; int predecessor;
     float err_coef;
-    int mode;
-    float* out_f; int out_stride;
-    const float* tau2;   // per slot
+    int k;
+    int nstages;
+    float* out_f;        // debug output
     int* surv; int* surv_cnt;
     int* status;
 };
 
 struct SmemLayout {
-    size_t stages, cand, bars, tmem_slot, total;
+    size_t stages, rec, heap, rowtau, bars, tmem_slot, total;
 };
-__host__ __device__ inline SmemLayout smem_layout() {
+__host__ __device__ inline SmemLayout smem_layout(int k, int nstages) {
     SmemLayout L;
     size_t off = 0;
-    L.stages = off; off += (size_t)STAGES * STAGE_BYTES;
-    L.cand = off;
-    L.bars = off; off += (size_t)(2 * STAGES + 4 + 1) * 8;
+    L.stages = off; off += (size_t)nstages * STAGE_BYTES;
+    L.rec = off; off += (size_t)2 * TC * REC * sizeof(float);
+    L.heap = off; off += (size_t)kEpiThreads * (k > 0 ? k : 1) * sizeof(float);
+    L.rowtau = off; off += (size_t)TQ * sizeof(unsigned long long);
+    L.bars = off; off += (size_t)(2 * STAGES + 4 + 4 + 1) * 8;
     L.tmem_slot = off; off += 16;
     L.total = off + 1024;  // alignment slack
     return L;
 }
 
-// Certified squared-distance bounds of one pair from the screened dot s.
-// xc: candidate scaled coordinates, vnc = ||v_c|| (rounded up), isc = 1/sqrt(p_c),
-// xmc = max |xs_c|.
-__device__ __forceinline__ void pair_bounds(float s, const float (&xq)[kMaxD], float vnq, float isq, float xmq,
-                                            const float (&xc)[kMaxD], float vnc, float isc, float xmc, int d,
-                                            float var, int kt, float err_coef, float& dl2, float& du2) {
-    float d2 = 0.f, sabs = 0.f;
-#pragma unroll
-    for (int c = 0; c < kMaxD; ++c) {
-        if (c < d) {
-            float t = xq[c] - xc[c];
-            d2 = fmaf(t, t, d2);
-            sabs += fabsf(t);
-        }
+// Max-heap of floats stored strided (element i of thread t at h[i * kEpiThreads]).
+__device__ __forceinline__ void heap_sift_down(float* h, int n, float x) {
+    int i = 0;
+    for (;;) {
+        int l = 2 * i + 1;
+        if (l >= n) break;
+        int r = l + 1;
+        int c = (r < n && h[r * kEpiThreads] > h[l * kEpiThreads]) ? r : l;
+        if (h[c * kEpiThreads] <= x) break;
+        h[i * kEpiThreads] = h[c * kEpiThreads];
+        i = c;
     }
-    // error of d2: rounding of the sum of squares + rounding of the scaled coordinates
-    float ed2 = (float)(d + 2) * 5.97e-8f * d2 + 2.39e-7f * sabs * (xmq + xmc);
-    float kv, ek;
-    if (kt == 0) {
-        kv = var * expf(-0.5f * d2);
-        ek = kv * (1e-6f + 0.5f * ed2);
-    } else {
-        float r = sqrtf(d2);
-        float a = 2.2360679775f * r;
-        float ea = expf(-a);
-        kv = var * (1.f + a + a * a * 0.33333334f) * ea;
-        // |dK/dd2| = var (5/6)(1+a) e^-a ; rounding of a, poly and exp bounded by 1e-6 K + a^2 term
-        ek = kv * 1e-6f + var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
+    h[i * kEpiThreads] = x;
+}
+__device__ __forceinline__ void heap_push(float* h, int n, float x) {
+    int i = n;
+    while (i > 0) {
+        int pnt = (i - 1) >> 1;
+        if (h[pnt * kEpiThreads] >= x) break;
+        h[i * kEpiThreads] = h[pnt * kEpiThreads];
+        i = pnt;
     }
-    float R = fabsf(kv - s);
-    float e = err_coef * vnq * vnc + ek + R * 1.2e-7f + 1e-30f;
-    float sc = isq * isc;
-    float rho_hi = (R + e) * sc * (1.f + 1e-6f);
-    float rho_lo = fmaxf(R - e, 0.f) * sc * (1.f - 1e-6f);
-    dl2 = 1.f - fminf(rho_hi, 1.f);
-    du2 = 1.f - fminf(rho_lo, 1.f);
+    h[i * kEpiThreads] = x;
 }
 
-__global__ void __launch_bounds__(kThreads, 1) screen_mma_kernel(MMAParams P) {
+// bit 2 of `which`: a kept job whose candidate tile already fed the heap during warm-up
+__device__ __forceinline__ bool jb_warm_seen(const Job& jb) { return (jb.which & 4) != 0; }
+
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    const SmemLayout L = smem_layout();
+    const SmemLayout L = smem_layout(P.k, P.nstages);
+    const int NS = P.nstages;
     unsigned char* stage_base = smem + L.stages;
+    float* recs = (float*)(smem + L.rec);
+    float* heaps = (float*)(smem + L.heap);
+    unsigned long long* rowtau = (unsigned long long*)(smem + L.rowtau);
     uint64_t* full = (uint64_t*)(smem + L.bars);
-    uint64_t* empty = full + STAGES;
+    uint64_t* empty = full + STAGES;  // barrier slots sized for the maximum stage count
     uint64_t* accf = empty + STAGES;
     uint64_t* acce = accf + 2;
-    uint64_t* done = acce + 2;
+    uint64_t* recf = acce + 2;
+    uint64_t* rece = recf + 2;
+    uint64_t* done = rece + 2;
     uint32_t* tmem_slot = (uint32_t*)(smem + L.tmem_slot);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nchunks = P.m / KC;
     const uint32_t idesc = sm::idesc_bf16_f32(TQ, TC);
+    const int jb0 = P.cta_job_begin[blockIdx.x], jb1 = P.cta_job_begin[blockIdx.x + 1];
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES; ++s) { sm::mbar_init(&full[s], 1); sm::mbar_init(&empty[s], 1); }
-        for (int a = 0; a < 2; ++a) { sm::mbar_init(&accf[a], 1); sm::mbar_init(&acce[a], kEpiWarps); }
+        for (int s = 0; s < NS; ++s) { sm::mbar_init(&full[s], 1); sm::mbar_init(&empty[s], 1); }
+        for (int a = 0; a < 2; ++a) {
+            sm::mbar_init(&accf[a], 1); sm::mbar_init(&acce[a], kEpiWarps);
+            sm::mbar_init(&recf[a], 1); sm::mbar_init(&rece[a], kEpiWarps);
+        }
         sm::mbar_init(done, 1);
         sm::fence_barrier_init();
     }
+    for (int r = threadIdx.x; r < TQ; r += blockDim.x) rowtau[r] = 0ULL;
     if (warp == 1) {
         sm::tmem_alloc(tmem_slot, 512);
         sm::tmem_relinquish();
@@ -176,20 +194,23 @@ __global__ void __launch_bounds__(kThreads, 1) screen_mma_kernel(MMAParams P) {
         // ------------------------------------------------------------ producer
         if (lane == 0) {
             long long it = 0;
-            for (int j = blockIdx.x; j < P.njobs; j += gridDim.x) {
+            for (int j = jb0; j < jb1; ++j) {
                 const Job jb = P.jobs[j];
+                const bf16* bh = P.b_hi[jb.which & 1];
+                const bf16* bl = P.b_lo[jb.which & 1];
+                const long long bg = P.b_groups[jb.which & 1];
                 for (int c = 0; c < nchunks; ++c, ++it) {
-                    const int s = (int)(it % STAGES);
-                    const unsigned ph = (unsigned)((it / STAGES) & 1);
+                    const int s = (int)(it % NS);
+                    const unsigned ph = (unsigned)((it / NS) & 1);
                     if (!sm::mbar_wait(&empty[s], ph ^ 1u, P.status, 11)) goto producer_done;
                     unsigned char* dst = stage_base + (size_t)s * STAGE_BYTES;
                     sm::mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
                     const size_t aoff = blocked_offset((long long)jb.qtile * TQ, c * KC, P.a_groups);
-                    const size_t boff = blocked_offset((long long)jb.ctile * TC, c * KC, P.b_groups);
+                    const size_t boff = blocked_offset((long long)jb.ctile * TC, c * KC, bg);
                     sm::bulk_g2s(dst, P.a_hi + aoff, CHUNK_A, &full[s]);
                     sm::bulk_g2s(dst + CHUNK_A, P.a_lo + aoff, CHUNK_A, &full[s]);
-                    sm::bulk_g2s(dst + 2 * CHUNK_A, P.b_hi + boff, CHUNK_B, &full[s]);
-                    sm::bulk_g2s(dst + 2 * CHUNK_A + CHUNK_B, P.b_lo + boff, CHUNK_B, &full[s]);
+                    sm::bulk_g2s(dst + 2 * CHUNK_A, bh + boff, CHUNK_B, &full[s]);
+                    sm::bulk_g2s(dst + 2 * CHUNK_A + CHUNK_B, bl + boff, CHUNK_B, &full[s]);
                 }
             }
         producer_done:;
@@ -199,7 +220,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_mma_kernel(MMAParams P) {
         if (lane == 0) {
             long long it = 0;
             int lt = 0;
-            for (int j = blockIdx.x; j < P.njobs; j += gridDim.x, ++lt) {
+            for (int j = jb0; j < jb1; ++j, ++lt) {
                 const int acc = lt & 1;
                 const unsigned aph = (unsigned)((lt >> 1) & 1);
                 if (!sm::mbar_wait(&acce[acc], aph ^ 1u, P.status, 12)) break;
@@ -207,8 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1) screen_mma_kernel(MMAParams P) {
                 const uint32_t dt = tmem_base + (uint32_t)(acc * TC);
                 bool ok = true;
                 for (int c = 0; c < nchunks; ++c, ++it) {
-                    const int s = (int)(it % STAGES);
-                    const unsigned ph = (unsigned)((it / STAGES) & 1);
+                    const int s = (int)(it % NS);
+                    const unsigned ph = (unsigned)((it / NS) & 1);
                     if (!sm::mbar_wait(&full[s], ph, P.status, 13)) { ok = false; break; }
                     sm::tc_fence_after();
                     unsigned char* st = stage_base + (size_t)s * STAGE_BYTES;
@@ -227,84 +248,156 @@ __global__ void __launch_bounds__(kThreads, 1) screen_mma_kernel(MMAParams P) {
                 if (!ok) break;
                 sm::mma_commit(&accf[acc]);
             }
-            // drain: every MMA issued by this thread has completed once `done` flips
             sm::mma_commit(done);
             sm::mbar_wait(done, 0, P.status, 14);
         }
+    } else if (warp == 2) {
+        // ------------------------------------------------------------ candidate staging
+        if (MODE == MODE_SWEEP) {
+            int lt = 0;
+            for (int j = jb0; j < jb1; ++j, ++lt) {
+                const Job jb = P.jobs[j];
+                const int acc = lt & 1;
+                const unsigned aph = (unsigned)((lt >> 1) & 1);
+                if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) break;
+                float* r = recs + (size_t)acc * TC * REC;
+                const int* bid = P.b_id[jb.which & 1];
+                for (int e = lane; e < TC; e += 32) {
+                    const int cid = bid[(long long)jb.ctile * TC + e];
+                    float* o = r + e * REC;
+                    if (cid >= 0) {
+#pragma unroll
+                        for (int c = 0; c < kMaxD; ++c) o[c] = c < P.d ? P.xs[(size_t)cid * P.d + c] : 0.f;
+                        o[8] = P.vn[cid]; o[9] = P.isp[cid]; o[10] = P.xmax[cid]; o[11] = __int_as_float(cid);
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < 11; ++c) o[c] = 0.f;
+                        o[11] = __int_as_float(-1);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) sm::mbar_arrive(&recf[acc]);
+            }
+        }
     } else {
         // ------------------------------------------------------------ epilogue
+        // Thread (row, half) owns the pairs of one query row with the 128 candidate
+        // columns of its half: its own heap, threshold and survivor segment, so no
+        // state is shared between warps.
+        const int ew = warp - 3;
         const int quarter = warp & 3;        // TMEM lanes 32*quarter ..
-        const int half = (warp - 2) >> 2;    // columns half*128 ..
+        const int half = ew >> 2;            // columns half*128 ..
         const int row = quarter * 32 + lane;
+        const int et = ew * 32 + lane;       // 0 .. kEpiThreads-1
+        float* heap = heaps + et;
         int lt = 0;
-        for (int j = blockIdx.x; j < P.njobs; j += gridDim.x, ++lt) {
+        int slot = -1, qid = -1, hn = 0, cnt = 0;
+        unsigned gen = 0;  // query-tile generation, tags the shared row threshold
+        float tau2 = 1.f;
+        float xq[kMaxD];
+        float cq = 0.f, isq = 0.f, xmq = 0.f;
+#pragma unroll
+        for (int c = 0; c < kMaxD; ++c) xq[c] = 0.f;
+        for (int j = jb0; j < jb1; ++j, ++lt) {
             const Job jb = P.jobs[j];
             const int acc = lt & 1;
             const unsigned aph = (unsigned)((lt >> 1) & 1);
-            const long long arow = (long long)jb.qtile * TQ + row;
-            const int slot = P.mode != MODE_DEBUG ? P.a_slot[arow] : -1;
-            const int qid = slot >= 0 ? P.slot_id[slot] : -1;
-            float xq[kMaxD];
-            float vnq = 0.f, isq = 0.f, xmq = 0.f, tau2 = -1.f;
+            if (MODE == MODE_SWEEP && jb.first) {
+                if (slot >= 0) P.surv_cnt[2 * slot + half] = cnt;
+                const long long arow = (long long)jb.qtile * TQ + row;
+                slot = P.a_slot[arow];
+                qid = slot >= 0 ? P.slot_id[slot] : -1;
+                hn = 0; cnt = 0; tau2 = 1.f; ++gen;
+                if (qid >= 0) {
+                    cq = P.err_coef * P.vn[qid]; isq = P.isp[qid]; xmq = P.xmax[qid];
 #pragma unroll
-            for (int c = 0; c < kMaxD; ++c) xq[c] = 0.f;
-            if (qid >= 0) {
-                vnq = P.vn[qid]; isq = P.isp[qid]; xmq = P.xmax[qid];
-#pragma unroll
-                for (int c = 0; c < kMaxD; ++c) if (c < P.d) xq[c] = P.xs[(size_t)qid * P.d + c];
-                if (P.mode == MODE_FILTER) tau2 = P.tau2[slot];
+                    for (int c = 0; c < kMaxD; ++c) xq[c] = c < P.d ? P.xs[(size_t)qid * P.d + c] : 0.f;
+                }
             }
+            if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) break;
             if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) break;
             sm::tc_fence_after();
+            const float* rb = recs + (size_t)acc * TC * REC;
             for (int cc = 0; cc < 4; ++cc) {
                 float v[32];
                 const int col0 = half * 128 + cc * 32;
                 sm::tmem_ld32(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TC + col0), v);
-                if (P.mode == MODE_DEBUG) {
-                    float* o = P.out_f + ((size_t)j * TQ + row) * TC + col0;
+                if (MODE == MODE_DEBUG) {
+                    float* o = P.out_f + ((size_t)(j - jb0) * TQ + row) * TC + col0;
 #pragma unroll
                     for (int i = 0; i < 32; ++i) o[i] = v[i];
                     continue;
                 }
-                // lane i holds the record of candidate col0 + i; broadcast by shuffles
-                const long long brow = (long long)jb.ctile * TC + col0 + lane;
-                const int my_cid = P.b_id[brow];
-                float my_vn = 0.f, my_isp = 0.f, my_xm = 0.f;
-                float my_x[kMaxD];
-#pragma unroll
-                for (int c = 0; c < kMaxD; ++c) my_x[c] = 0.f;
-                if (my_cid >= 0) {
-                    my_vn = P.vn[my_cid]; my_isp = P.isp[my_cid]; my_xm = P.xmax[my_cid];
-#pragma unroll
-                    for (int c = 0; c < kMaxD; ++c) if (c < P.d) my_x[c] = P.xs[(size_t)my_cid * P.d + c];
+                if (qid < 0) continue;
+                const bool keep = !(jb.which & 2);
+                {   // the other half's threshold, when it belongs to this query tile
+                    const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
+                    if ((unsigned)(w >> 32) == gen) tau2 = fminf(tau2, __uint_as_float(~(unsigned)w));
                 }
-#pragma unroll 2
-                for (int i = 0; i < 32; ++i) {
-                    const int cid = __shfl_sync(0xffffffffu, my_cid, i);
-                    const float vnc = __shfl_sync(0xffffffffu, my_vn, i);
-                    const float isc = __shfl_sync(0xffffffffu, my_isp, i);
-                    const float xmc = __shfl_sync(0xffffffffu, my_xm, i);
-                    float xc[kMaxD];
 #pragma unroll
-                    for (int c = 0; c < kMaxD; ++c) xc[c] = __shfl_sync(0xffffffffu, my_x[c], i);
-                    if (qid < 0) continue;
-                    const bool valid = cid >= 0 && (!P.predecessor || cid < qid);
+                for (int i = 0; i < 32; ++i) {
+                    const float4* r4 = (const float4*)(rb + (col0 + i) * REC);
+                    const float4 xa = r4[0], xb = r4[1], meta = r4[2];
+                    const int cid = __float_as_int(meta.w);
+                    if (cid < 0 || (P.predecessor && cid >= qid)) continue;
                     float dl2 = 0.f, du2 = 0.f;
-                    if (valid && cid != qid)
-                        pair_bounds(v[i], xq, vnq, isq, xmq, xc, vnc, isc, xmc, P.d, P.var, P.kernel_type,
-                                    P.err_coef, dl2, du2);
-                    if (P.mode == MODE_WINDOW) {
-                        P.out_f[(size_t)slot * P.out_stride + (size_t)jb.slot * TC + col0 + i] = valid ? du2 : 2.0f;
-                    } else if (valid && dl2 <= tau2) {
-                        int k = atomicAdd(&P.surv_cnt[slot], 1);
-                        if (k < SURV_CAP) P.surv[(size_t)slot * SURV_CAP + k] = cid;
+                    if (cid != qid) {
+                        const float xc[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+                        float d2 = 0.f;
+#pragma unroll
+                        for (int c = 0; c < kMaxD; ++c) { float t = xq[c] - xc[c]; d2 = fmaf(t, t, d2); }
+                        // error of d2: rounding of the sum and of the scaled coordinates
+                        const float ed2 = (float)(P.d + 2) * 5.97e-8f * d2 +
+                                          4.8e-7f * sqrtf((float)P.d * d2) * (xmq + meta.z);
+                        float kv, ek;
+                        if (P.kernel_type == 0) {
+                            const float x = -0.5f * d2;
+                            kv = P.var * __expf(x);
+                            ek = kv * (1e-6f + 1.2e-7f * fabsf(x) + 0.5f * ed2);
+                        } else {
+                            const float a = 2.2360679775f * sqrtf(d2);
+                            const float ea = __expf(-a);
+                            kv = P.var * (1.f + a + a * a * 0.33333334f) * ea;
+                            ek = kv * (1e-6f + 2.4e-7f * a) + P.var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
+                        }
+                        const float R = fabsf(kv - v[i]);
+                        const float e = cq * meta.x + ek + R * 1.2e-7f + 1e-30f;
+                        const float sc = isq * meta.y;
+                        dl2 = 1.f - fminf((R + e) * sc * (1.f + 1e-6f), 1.f);
+                        du2 = 1.f - fminf(fmaxf(R - e, 0.f) * sc * (1.f - 1e-6f), 1.f);
+                    }
+                    if (keep && dl2 <= tau2) {
+                        if (cnt < HALF_CAP) P.surv[((size_t)slot * 2 + half) * HALF_CAP + cnt] = cid;
+                        ++cnt;
+                    }
+                    // running k smallest upper bounds of this row half -> tau2.  Warm-up
+                    // jobs repeat later as kept jobs, so they only feed the heap once.
+                    if (!keep || !jb_warm_seen(jb)) {
+                        if (hn < P.k) {
+                            heap_push(heap, hn, du2);
+                            ++hn;
+                            if (hn == P.k && heap[0] < tau2) {
+                                tau2 = heap[0];
+                                atomicMax(&rowtau[row], ((unsigned long long)gen << 32) | (unsigned long long)(~__float_as_uint(tau2)));
+                            }
+                        } else if (du2 < heap[0]) {
+                            heap_sift_down(heap, hn, du2);
+                            if (heap[0] < tau2) {
+                                tau2 = heap[0];
+                                atomicMax(&rowtau[row], ((unsigned long long)gen << 32) | (unsigned long long)(~__float_as_uint(tau2)));
+                            }
+                        }
                     }
                 }
             }
             sm::tc_fence_before();
             __syncwarp();
-            if (lane == 0) sm::mbar_arrive(&acce[acc]);
+            if (lane == 0) {
+                sm::mbar_arrive(&acce[acc]);
+                if (MODE == MODE_SWEEP) sm::mbar_arrive(&rece[acc]);
+            }
         }
+        if (MODE == MODE_SWEEP && slot >= 0) P.surv_cnt[2 * slot + half] = cnt;
     }
     sm::tc_fence_before();
     __syncthreads();
@@ -377,28 +470,6 @@ __device__ __forceinline__ unsigned long long pack_key(float d, int id) {
     return ((unsigned long long)__float_as_uint(d) << 32) | (unsigned)id;
 }
 
-// tau2[slot] = k-th smallest certified upper bound in the slot's window row.
-__global__ void window_tau_kernel(const float* __restrict__ win, int width, const int* __restrict__ a_slot,
-                                  long long a_rows, int k, float* __restrict__ tau2) {
-    extern __shared__ unsigned long long skeys[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned long long* keys = skeys + (size_t)warp * RBUF;
-    long long row = (long long)blockIdx.x * (blockDim.x / 32) + warp;
-    if (row >= a_rows) return;
-    int slot = a_slot[row];
-    if (slot < 0) return;
-    for (int i = lane; i < RBUF; i += 32) {
-        float v = i < width ? win[(size_t)slot * width + i] : 2.0f;
-        keys[i] = pack_key(v, i);
-    }
-    __syncwarp();
-    warp_bitonic_sort(keys);
-    if (lane == 0) {
-        float t = __uint_as_float((unsigned)(keys[k - 1] >> 32));
-        tau2[slot] = t > 1.0f ? 1.0f : t;   // fewer than k valid: no pruning
-    }
-}
-
 // ------------------------------------------------------------------ rescoring
 struct RescoreParams {
     const float* v; int m;          // natural layout, dataset order
@@ -415,10 +486,10 @@ struct RescoreParams {
     long long* evals;
 };
 
-// FP64-grade residual distance of (q, c): compensated FP32 dot (TwoProd via FMA,
-// TwoSum), FP64 kernel value, normalisation and square root.  The warp holds
-// the query row as vq[t] = v_q[32 t + lane] (m <= 1024).
-__device__ __forceinline__ float exact_distance(const RescoreParams& P, int q, int c, const float (&vq)[32]) {
+// Compensated FP32 dot product v_q . v_c (TwoProd via FMA, TwoSum), reduced
+// across the warp in FP64.  The warp holds the query row as vq[t] = v_q[32 t + lane]
+// (m <= 1024).  Every lane returns the full sum.
+__device__ __forceinline__ double warp_dot_compensated(const RescoreParams& P, int c, const float (&vq)[32]) {
     const int lane = threadIdx.x & 31;
     float s = 0.f, comp = 0.f;
     const float* vc = P.v + (size_t)c * P.m;
@@ -426,7 +497,7 @@ __device__ __forceinline__ float exact_distance(const RescoreParams& P, int q, i
     for (int t = 0; t < 32; ++t) {
         const int e = t * 32 + lane;
         if (e < P.m) {
-            float a = vq[t], b = vc[e];
+            float a = vq[t], b = __ldg(vc + e);
             float pr = a * b;
             float pe = fmaf(a, b, -pr);
             float ts = s + pr;
@@ -439,6 +510,11 @@ __device__ __forceinline__ float exact_distance(const RescoreParams& P, int q, i
     double dot = (double)s + (double)comp;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
+    return dot;
+}
+
+// FP64 kernel value, normalisation and square root for one pair (one lane).
+__device__ __forceinline__ float exact_from_dot(const RescoreParams& P, int q, int c, double dot) {
     if (q == c) return 0.f;
     double d2 = 0.0;
     for (int a = 0; a < P.d; ++a) {
@@ -473,8 +549,14 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
     long long nwork = use_full ? P.nfull : P.nslots;
     if (w >= nwork) return;
     const int slot = use_full ? P.full_slots[w] : (int)w;
-    if (!use_full && P.surv_cnt[slot] > SURV_CAP) return;  // handled by the full pass
+    const int c0 = use_full ? 0 : P.surv_cnt[2 * slot];
+    const int c1 = use_full ? 0 : P.surv_cnt[2 * slot + 1];
+    if (!use_full && (c0 > HALF_CAP || c1 > HALF_CAP)) return;  // handled by the exhaustive pass
     const int q = P.slot_id[slot];
+    if (q < 0) {
+        for (int j = lane; j < P.k; j += 32) { P.out_idx[(size_t)slot * P.k + j] = -1; P.out_dist[(size_t)slot * P.k + j] = CT_FLT_MAX; }
+        return;
+    }
     const int k = P.k;
     // query row slice held per lane
     float vql[32];
@@ -482,21 +564,25 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
     for (int t = 0; t < 32; ++t) vql[t] = (t * 32 + lane < P.m) ? P.v[(size_t)q * P.m + t * 32 + lane] : 0.f;
     for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
     __syncwarp();
-    long long count = use_full ? (P.predecessor ? (long long)q : P.n) : (long long)P.surv_cnt[slot];
+    long long count = use_full ? (P.predecessor ? (long long)q : P.n) : (long long)(c0 + c1);
     int fill = k;  // next free position in the buffer
     long long evals = 0;
     for (long long base = 0; base < count; base += 32) {
         // each lane fetches one candidate id; the warp scores them one at a time
         long long ci = base + lane;
         int cid = -1;
-        if (ci < count) cid = use_full ? (int)ci : P.surv[(size_t)slot * SURV_CAP + ci];
-        float mydist = 0.f;
+        if (ci < count)
+            cid = use_full ? (int)ci
+                           : (ci < c0 ? P.surv[(size_t)(2 * slot) * HALF_CAP + ci]
+                                      : P.surv[(size_t)(2 * slot + 1) * HALF_CAP + (ci - c0)]);
+        double mydot = 0.0;
         const int nb = (int)((count - base) < 32 ? (count - base) : 32);
         for (int t = 0; t < nb; ++t) {
             int c = __shfl_sync(0xffffffffu, cid, t);
-            float dist = exact_distance(P, q, c, vql);
-            if (lane == t) mydist = dist;
+            double dot = warp_dot_compensated(P, c, vql);
+            if (lane == t) mydot = dot;
         }
+        float mydist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
         evals += nb;
         // append to buffer
         bool has = ci < count;
@@ -530,17 +616,9 @@ __global__ void collect_overflow_kernel(const int* __restrict__ surv_cnt, long l
                                         int* __restrict__ nlist) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= nslots) return;
-    if (surv_cnt[s] > SURV_CAP) list[atomicAdd(nlist, 1)] = (int)s;
+    if (surv_cnt[2 * s] > HALF_CAP || surv_cnt[2 * s + 1] > HALF_CAP) list[atomicAdd(nlist, 1)] = (int)s;
 }
 
-__global__ void debug_jobs_kernel(Job* jobs, int njobs, int nqt, int nct) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= njobs) return;
-    jobs[j].qtile = j / nct;
-    jobs[j].ctile = j % nct;
-    jobs[j].slot = 0;
-    jobs[j].pad = 0;
-}
 
 }  // namespace screen
 }  // namespace ct
@@ -549,19 +627,33 @@ __global__ void debug_jobs_kernel(Job* jobs, int njobs, int nqt, int nct) {
 namespace ct {
 namespace screen {
 
+// One "level" of the threshold pass: the points of a prefix [0, P) of the
+// dataset (P = 2^j), or the whole dataset, in Hilbert order.  Predecessor-mode
+// query q uses the largest prefix level with P <= q, so every candidate of its
+// window is a valid predecessor.
+struct Level {
+    long long size = 0, row_off = 0, rows_pad = 0;
+};
+
 struct State {
     long long n = 0, rows_pad = 0;        // candidate rows padded to TC
     int* hil_order = nullptr;             // sorted position -> dataset id
-    int* hil_pos = nullptr;               // dataset id -> sorted position
+    unsigned long long* hil_key = nullptr;  // Hilbert key by dataset id
     bf16 *ds_hi = nullptr, *ds_lo = nullptr;    // dataset order, blocked
-    bf16 *hil_hi = nullptr, *hil_lo = nullptr;  // Hilbert order, blocked
     int* b_id_ds = nullptr;
-    int* b_id_hil = nullptr;
+    // threshold-pass levels, concatenated in one blocked matrix
+    std::vector<Level> levels;
+    long long lvl_rows = 0;
+    bf16 *lvl_hi = nullptr, *lvl_lo = nullptr;
+    int* lvl_id = nullptr;                  // row -> dataset id (-1 padding)
+    unsigned long long* lvl_key = nullptr;  // row -> Hilbert key (UINT64_MAX padding)
+    long long* lvl_meta = nullptr;          // [nlevels][3]: size, row_off, rows_pad
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
     double* inv_ls64 = nullptr;
     int* status = nullptr;
-    std::vector<int> hil_order_host;
 };
+
+constexpr int kFirstPrefixLog2 = 10;  // prefixes below 1024 points: every predecessor is rescored
 
 __global__ void iota_kernel(int* a, long long n, long long valid) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -575,20 +667,53 @@ __global__ void inverse_perm_kernel(const int* order, long long n, int* inv) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) inv[order[i]] = (int)i;
 }
-// slot ids from int64 query ids; out-of-range ids become -1
+// slot ids from int64 query ids (out-of-range ids become -1) and the sweep sort
+// key: high 32 bits = group (predecessor mode: level and one of kBands id bands
+// of the level's query range), low 32 bits = row of the query's Hilbert
+// position inside its level.  Queries without a level sort last.
+constexpr int kBands = 16;
+constexpr int kWarmTiles = 16;  // nearest candidate tiles that set the thresholds before any pair is kept
 __global__ void slot_ids_kernel(const long long* q, long long nq, long long n, int* slot_id,
-                                unsigned long long* key_ds, unsigned long long* key_hil, int* val_ds, int* val_hil,
-                                const int* hil_pos) {
+                                unsigned long long* key_lvl, int* val_lvl, const unsigned long long* hil_key,
+                                const unsigned long long* lvl_key, const long long* lvl_meta, int nlevels,
+                                int predecessor) {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= nq) return;
     long long id = q[i];
     bool ok = id >= 0 && id < n;
     slot_id[i] = ok ? (int)id : -1;
-    key_ds[i] = ok ? (unsigned long long)id : (unsigned long long)n;
-    key_hil[i] = ok ? (unsigned long long)hil_pos[id] : (unsigned long long)n;
-    val_ds[i] = (int)i;
-    val_hil[i] = (int)i;
+    val_lvl[i] = (int)i;
+    unsigned long long kl = 0xFFFFFFFFFFFFFFFFULL;
+    if (ok) {
+        int li = -1;
+        if (!predecessor) {
+            li = nlevels - 1;  // whole dataset
+        } else {
+            for (int l = 0; l < nlevels - 1; ++l)
+                if (lvl_meta[3 * l] <= id) li = l;
+        }
+        if (li >= 0) {
+            const long long off = lvl_meta[3 * li + 1], size = lvl_meta[3 * li];
+            const unsigned long long key = hil_key[id];
+            long long lo = 0, hi = size;  // first row with key >= query key
+            while (lo < hi) {
+                long long mid = (lo + hi) >> 1;
+                if (lvl_key[off + mid] < key) lo = mid + 1; else hi = mid;
+            }
+            if (lo >= size) lo = size - 1;
+            long long band = 0;
+            if (predecessor) band = ((id - size) * kBands) / size;  // ids of this level lie in [size, 2 size)
+            if (band < 0) band = 0;
+            if (band >= kBands) band = kBands - 1;
+            const unsigned long long group = (unsigned long long)(li * kBands + band);
+            kl = (group << 32) | (unsigned long long)(off + lo);
+        } else {
+            kl = (0xFFFFFFFEULL << 32) | (unsigned long long)id;  // no level: by id
+        }
+    }
+    key_lvl[i] = kl;
 }
+
 // rowmap (A row -> dataset row) and a_slot (A row -> slot) from a sorted slot list
 __global__ void arows_kernel(const int* sorted_slots, long long nq, long long rows, const int* slot_id, int* a_slot,
                              int* rowmap) {
@@ -607,16 +732,26 @@ static float err_coef_for(int m) {
     return (float)(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * std::ldexp(1.0, -22));
 }
 
-static cudaError_t launch_mma(const MMAParams& P, cudaStream_t st) {
-    const size_t smem = smem_layout().total;
-    cudaError_t e = cudaFuncSetAttribute(screen_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int grid = P.njobs < sms ? P.njobs : sms;
-    if (grid <= 0) return cudaSuccess;
-    screen_mma_kernel<<<grid, kThreads, smem, st>>>(P);
+static int pick_stages(int k) {
+    for (int ns = STAGES; ns >= 2; --ns)
+        if (smem_layout(k, ns).total <= 232448) return ns;
+    return 0;
+}
+
+// ncta CTAs, CTA c runs jobs [cta_begin[c], cta_begin[c+1]).
+static cudaError_t launch_sweep(const MMAParams& P, int mode, int ncta, cudaStream_t st) {
+    if (ncta <= 0) return cudaSuccess;
+    const size_t smem = smem_layout(P.k, P.nstages).total;
+    cudaError_t e;
+    if (mode == MODE_DEBUG) {
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_DEBUG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        screen_sweep_kernel<MODE_DEBUG><<<ncta, kThreads, smem, st>>>(P);
+    } else {
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        screen_sweep_kernel<MODE_SWEEP><<<ncta, kThreads, smem, st>>>(P);
+    }
     return cudaGetLastError();
 }
 
@@ -628,14 +763,17 @@ using namespace ct::screen;
 void ct_tree::release_screen() {
     State* S = (State*)screen;
     if (!S) return;
-    cudaFree(S->hil_order); cudaFree(S->hil_pos); cudaFree(S->ds_hi); cudaFree(S->ds_lo);
-    cudaFree(S->hil_hi); cudaFree(S->hil_lo); cudaFree(S->b_id_ds); cudaFree(S->b_id_hil);
+    cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
+    cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
     delete S;
     screen = nullptr;
 }
 
-// Build the screened-form operands once per tree (lazily, on first use).
+// Build the screened-form operands once per tree (lazily, on first use):
+// dataset-order blocked hi/lo V for the main sweep, the Hilbert order and keys,
+// and the threshold levels (prefixes 2^10, 2^11, ... < n and the whole set),
+// each in Hilbert order, concatenated into one blocked matrix.
 static int screen_prepare(ct_tree* T, cudaStream_t st) {
     if (T->screen) return CT_OK;
     State* S = new State();
@@ -644,30 +782,61 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     S->n = n;
     S->rows_pad = ((n + TC - 1) / TC) * TC;
     const int m = T->m;
+    for (int j = kFirstPrefixLog2; (1LL << j) < n; ++j) {
+        Level L; L.size = 1LL << j; S->levels.push_back(L);
+    }
+    { Level L; L.size = n; S->levels.push_back(L); }
+    long long off = 0;
+    for (auto& L : S->levels) { L.row_off = off; L.rows_pad = ((L.size + TC - 1) / TC) * TC; off += L.rows_pad; }
+    S->lvl_rows = off;
     cudaError_t e = cudaSuccess;
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 16); };
     A((void**)&S->hil_order, sizeof(int) * n);
-    A((void**)&S->hil_pos, sizeof(int) * n);
+    A((void**)&S->hil_key, sizeof(unsigned long long) * n);
     A((void**)&S->ds_hi, sizeof(bf16) * S->rows_pad * m);
     A((void**)&S->ds_lo, sizeof(bf16) * S->rows_pad * m);
-    A((void**)&S->hil_hi, sizeof(bf16) * S->rows_pad * m);
-    A((void**)&S->hil_lo, sizeof(bf16) * S->rows_pad * m);
     A((void**)&S->b_id_ds, sizeof(int) * S->rows_pad);
-    A((void**)&S->b_id_hil, sizeof(int) * S->rows_pad);
+    A((void**)&S->lvl_hi, sizeof(bf16) * S->lvl_rows * m);
+    A((void**)&S->lvl_lo, sizeof(bf16) * S->lvl_rows * m);
+    A((void**)&S->lvl_id, sizeof(int) * S->lvl_rows);
+    A((void**)&S->lvl_key, sizeof(unsigned long long) * S->lvl_rows);
+    A((void**)&S->lvl_meta, sizeof(long long) * 3 * S->levels.size());
     A((void**)&S->vn, sizeof(float) * n);
     A((void**)&S->isp, sizeof(float) * n);
     A((void**)&S->xmax, sizeof(float) * n);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->status, sizeof(int));
     if (e != cudaSuccess) return T->set_err(CT_ERR_NOMEM, "screen prep allocation: %s", cudaGetErrorString(e));
-    e = ct::compute_order(T->coords_raw, n, T->d, 1, S->hil_order, st);
+    e = ct::compute_order(T->coords_raw, n, T->d, 1, S->hil_order, st, S->hil_key);
+    std::vector<int> order_h(n);
+    std::vector<unsigned long long> key_h(n);
     if (e == cudaSuccess) {
-        inverse_perm_kernel<<<grid_for(n), 256, 0, st>>>(S->hil_order, n, S->hil_pos);
         iota_kernel<<<grid_for(S->rows_pad), 256, 0, st>>>(S->b_id_ds, S->rows_pad, n);
-        gather_ids_kernel<<<grid_for(S->rows_pad), 256, 0, st>>>(S->hil_order, n, S->rows_pad, S->b_id_hil);
         split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->b_id_ds, S->rows_pad, S->ds_hi, S->ds_lo);
-        split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->b_id_hil, S->rows_pad, S->hil_hi, S->hil_lo);
         point_scalars_kernel<<<grid_for(n), 256, 0, st>>>(T->vnat, T->p, T->xs, n, m, T->d, S->vn, S->isp, S->xmax);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(order_h.data(), S->hil_order, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(key_h.data(), S->hil_key, 8 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return T->set_err(CT_ERR_CUDA, "screen prep: %s", cudaGetErrorString(e));
+    // level rows: the Hilbert order filtered to ids < size (stable, so still key-sorted)
+    std::vector<int> lid(S->lvl_rows, -1);
+    std::vector<unsigned long long> lkey(S->lvl_rows, ~0ULL);
+    std::vector<long long> meta;
+    for (const auto& L : S->levels) {
+        long long r = L.row_off;
+        for (long long i = 0; i < n; ++i) {
+            int id = order_h[i];
+            if (id < L.size) { lid[r] = id; lkey[r] = key_h[id]; ++r; }
+        }
+        meta.push_back(L.size); meta.push_back(L.row_off); meta.push_back(L.rows_pad);
+    }
+    e = cudaMemcpyAsync(S->lvl_id, lid.data(), sizeof(int) * S->lvl_rows, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S->lvl_key, lkey.data(), 8 * S->lvl_rows, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(S->lvl_meta, meta.data(), sizeof(long long) * meta.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->lvl_id, S->lvl_rows, S->lvl_hi, S->lvl_lo);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -675,11 +844,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
         for (int i = 0; i < T->d; ++i) ils[i] = T->inv_ls_host64[i];
         e = cudaMemcpyAsync(S->inv_ls64, ils, sizeof(double) * T->d, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(int), st);
-        if (e == cudaSuccess) {
-            S->hil_order_host.resize(n);
-            e = cudaMemcpyAsync(S->hil_order_host.data(), S->hil_order, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
-        }
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors above go out of scope
     }
     if (e != cudaSuccess) return T->set_err(CT_ERR_CUDA, "screen prep: %s", cudaGetErrorString(e));
     return CT_OK;
@@ -689,141 +854,162 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
                           ct_stats* stats, cudaStream_t st) {
     if (d > kMaxD) return set_err(CT_ERR_UNSUPPORTED, "screened form supports d <= %d (got %d)", kMaxD, d);
     if (m % KC != 0 || m > 1024) return set_err(CT_ERR_UNSUPPORTED, "screened form needs m %% 32 == 0 and m <= 1024 (got %d)", m);
-    if (k > 512) return set_err(CT_ERR_UNSUPPORTED, "screened form supports k <= 512");
+    if (k > kMaxK) return set_err(CT_ERR_UNSUPPORTED, "screened form supports k <= %d (got %d)", kMaxK, k);
+    const int nstages = pick_stages(k);
+    if (nstages == 0) return set_err(CT_ERR_UNSUPPORTED, "screened form: k=%d does not fit shared memory", k);
     int rc = screen_prepare(this, st);
     if (rc != CT_OK) return rc;
     State* S = (State*)screen;
     const long long rows_q = ((nq + TQ - 1) / TQ) * TQ;
     const long long nqt = rows_q / TQ;
-    const long long nct = S->rows_pad / TC;
+    const int nlev = (int)S->levels.size();
     cudaError_t e = cudaSuccess;
+    const bool timing = ct::timing_enabled();
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (timing) {
+        for (int i = 0; i < 6; ++i) cudaEventCreate(&ev[i]);
+        cudaEventRecord(ev[0], st);
+    }
+    long long launches = 0;
     // ---- per-call buffers
-    int *slot_id = nullptr, *val_ds = nullptr, *val_hil = nullptr, *vtmp = nullptr;
-    unsigned long long *key_ds = nullptr, *key_hil = nullptr, *ktmp = nullptr;
+    int *slot_id = nullptr, *val_lvl = nullptr, *vtmp = nullptr;
+    unsigned long long *key_lvl = nullptr, *ktmp = nullptr;
     unsigned* hist = nullptr;
-    int *a_slot_ds = nullptr, *a_slot_hil = nullptr, *rowmap_ds = nullptr, *rowmap_hil = nullptr;
-    bf16 *aq_hi = nullptr, *aq_lo = nullptr, *ah_hi = nullptr, *ah_lo = nullptr;
-    float *win = nullptr, *tau2 = nullptr;
-    int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr;
+    int *a_slot_lvl = nullptr, *rowmap_lvl = nullptr;
+    bf16 *al_hi = nullptr, *al_lo = nullptr;
+    int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr, *cta_begin = nullptr;
     long long* evals_d = nullptr;
-    Job *jobs_a = nullptr, *jobs_b = nullptr;
+    Job* jobs = nullptr;
     const int nbh = ct::radix_num_blocks(nq);
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes ? bytes : 16, st); };
     A((void**)&slot_id, sizeof(int) * nq);
-    A((void**)&val_ds, sizeof(int) * nq); A((void**)&val_hil, sizeof(int) * nq); A((void**)&vtmp, sizeof(int) * nq);
-    A((void**)&key_ds, 8 * nq); A((void**)&key_hil, 8 * nq); A((void**)&ktmp, 8 * nq);
+    A((void**)&val_lvl, sizeof(int) * nq); A((void**)&vtmp, sizeof(int) * nq);
+    A((void**)&key_lvl, 8 * nq); A((void**)&ktmp, 8 * nq);
     A((void**)&hist, sizeof(unsigned) * 256 * (size_t)nbh);
-    A((void**)&a_slot_ds, sizeof(int) * rows_q); A((void**)&a_slot_hil, sizeof(int) * rows_q);
-    A((void**)&rowmap_ds, sizeof(int) * rows_q); A((void**)&rowmap_hil, sizeof(int) * rows_q);
-    A((void**)&win, sizeof(float) * nq * WINDOW_TILES * TC);
-    A((void**)&tau2, sizeof(float) * nq);
+    A((void**)&a_slot_lvl, sizeof(int) * rows_q);
+    A((void**)&rowmap_lvl, sizeof(int) * rows_q);
+    A((void**)&al_hi, sizeof(bf16) * rows_q * m); A((void**)&al_lo, sizeof(bf16) * rows_q * m);
     A((void**)&surv, sizeof(int) * nq * SURV_CAP);
-    A((void**)&surv_cnt, sizeof(int) * nq);
+    A((void**)&surv_cnt, sizeof(int) * 2 * nq);
     A((void**)&full_list, sizeof(int) * nq);
     A((void**)&nfull_d, sizeof(int));
     A((void**)&evals_d, sizeof(long long));
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
 
-    slot_ids_kernel<<<grid_for(nq), 256, 0, st>>>((const long long*)q_ids, nq, n, slot_id, key_ds, key_hil, val_ds,
-                                                 val_hil, S->hil_pos);
+    slot_ids_kernel<<<grid_for(nq), 256, 0, st>>>((const long long*)q_ids, nq, n, slot_id, key_lvl, val_lvl,
+                                                 S->hil_key, S->lvl_key, S->lvl_meta, nlev, predecessor ? 1 : 0);
+    ++launches;
     bool in_tmp = false;
-    int kb_ds = 0, kb_hil = 0;
-    for (long long t = n; t > 0; t >>= 1) ++kb_ds;
-    kb_hil = kb_ds;
-    e = ct::radix_sort_pairs(key_ds, val_ds, ktmp, vtmp, nq, kb_ds, hist, nullptr, 0, st, &in_tmp);
-    if (e == cudaSuccess && in_tmp) { e = cudaMemcpyAsync(val_ds, vtmp, sizeof(int) * nq, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(key_ds, ktmp, 8 * nq, cudaMemcpyDeviceToDevice, st); }
-    if (e == cudaSuccess) e = ct::radix_sort_pairs(key_hil, val_hil, ktmp, vtmp, nq, kb_hil, hist, nullptr, 0, st, &in_tmp);
-    if (e == cudaSuccess && in_tmp) { e = cudaMemcpyAsync(val_hil, vtmp, sizeof(int) * nq, cudaMemcpyDeviceToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(key_hil, ktmp, 8 * nq, cudaMemcpyDeviceToDevice, st); }
+    const int kb_lvl = 64;
+    launches += 3 * ((kb_lvl + 7) / 8) + 2;
+    e = ct::radix_sort_pairs(key_lvl, val_lvl, ktmp, vtmp, nq, kb_lvl, hist, nullptr, 0, st, &in_tmp);
+    if (e == cudaSuccess && in_tmp) { e = cudaMemcpyAsync(val_lvl, vtmp, sizeof(int) * nq, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(key_lvl, ktmp, 8 * nq, cudaMemcpyDeviceToDevice, st); }
     if (e == cudaSuccess) {
-        arows_kernel<<<grid_for(rows_q), 256, 0, st>>>(val_ds, nq, rows_q, slot_id, a_slot_ds, rowmap_ds);
-        arows_kernel<<<grid_for(rows_q), 256, 0, st>>>(val_hil, nq, rows_q, slot_id, a_slot_hil, rowmap_hil);
+        arows_kernel<<<grid_for(rows_q), 256, 0, st>>>(val_lvl, nq, rows_q, slot_id, a_slot_lvl, rowmap_lvl);
+        split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_lvl, rows_q, al_hi, al_lo);
         e = cudaGetLastError();
     }
-    // sorted keys to host to lay out the job lists
-    std::vector<unsigned long long> hk_ds(nq), hk_hil(nq);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hk_ds.data(), key_ds, 8 * nq, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(hk_hil.data(), key_hil, 8 * nq, cudaMemcpyDeviceToHost, st);
+    std::vector<unsigned long long> hk_lvl(nq);
+    std::vector<int> hrow_id(rows_q);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hk_lvl.data(), key_lvl, 8 * nq, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hrow_id.data(), rowmap_lvl, sizeof(int) * rows_q, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form setup: %s", cudaGetErrorString(e));
 
-    // ---- A operands: reuse the dataset blocks when the query set is 0..n-1
-    bool all_ds = nq == n, all_hil = nq == n;
-    for (long long i = 0; i < nq && all_ds; ++i) all_ds = hk_ds[i] == (unsigned long long)i;
-    for (long long i = 0; i < nq && all_hil; ++i) all_hil = hk_hil[i] == (unsigned long long)i;
-    const bf16 *Aq_hi = S->ds_hi, *Aq_lo = S->ds_lo, *Ah_hi = S->hil_hi, *Ah_lo = S->hil_lo;
-    long long gq = S->rows_pad / 8, gh = S->rows_pad / 8;
-    if (!all_ds) {
-        A((void**)&aq_hi, sizeof(bf16) * rows_q * m); A((void**)&aq_lo, sizeof(bf16) * rows_q * m);
-        if (e == cudaSuccess) split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_ds, rows_q, aq_hi, aq_lo);
-        Aq_hi = aq_hi; Aq_lo = aq_lo; gq = rows_q / 8;
-    }
-    if (!all_hil) {
-        A((void**)&ah_hi, sizeof(bf16) * rows_q * m); A((void**)&ah_lo, sizeof(bf16) * rows_q * m);
-        if (e == cudaSuccess) split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_hil, rows_q, ah_hi, ah_lo);
-        Ah_hi = ah_hi; Ah_lo = ah_lo; gh = rows_q / 8;
-    }
-    // ---- job lists
-    std::vector<Job> ja, jbv;
-    const int wt = nct < WINDOW_TILES ? (int)nct : WINDOW_TILES;
+    // ---- per query tile: candidate tiles nearest-first
+    std::vector<std::vector<Job>> tiles(nqt);
+    const long long n_ds_tiles = S->rows_pad / TC;
     for (long long t = 0; t < nqt; ++t) {
-        long long r = t * TQ + TQ / 2;
-        if (r >= nq) r = nq - 1;
-        long long pos = (long long)hk_hil[r];
-        if (pos >= n) pos = n - 1;
-        long long c0 = pos / TC - (wt - 1) / 2;
-        if (c0 < 0) c0 = 0;
-        if (c0 + wt > nct) c0 = nct - wt;
-        for (int w = 0; w < wt; ++w) ja.push_back(Job{(int)t, (int)(c0 + w), w, 0});
-    }
-    for (long long t = 0; t < nqt; ++t) {
-        long long last = (t + 1) * TQ - 1;
-        if (last >= nq) last = nq - 1;
-        long long maxid = (long long)hk_ds[last];
-        if (maxid >= n) {  // invalid ids sort last; use the last valid one
-            long long r = last;
-            while (r >= t * TQ && (long long)hk_ds[r] >= n) --r;
-            maxid = r >= t * TQ ? (long long)hk_ds[r] : -1;
+        long long maxq = -1;
+        for (long long r = t * TQ; r < (t + 1) * TQ; ++r) maxq = std::max<long long>(maxq, hrow_id[r]);
+        if (maxq < 0) continue;  // no valid query in this tile
+        long long r = std::min<long long>(t * TQ + TQ / 2, nq - 1);
+        auto row_of = [&](long long rr) -> long long {
+            unsigned long long key = hk_lvl[rr];
+            if ((key >> 32) >= 0xFFFFFFFEULL) return -1;
+            return (long long)(key & 0xFFFFFFFFULL);
+        };
+        long long row = row_of(r);
+        if (row < 0) row = row_of(t * TQ);
+        std::vector<Job>& J = tiles[t];
+        int li = -1;
+        if (row >= 0)
+            for (int l = 0; l < nlev; ++l)
+                if (row >= S->levels[l].row_off && row < S->levels[l].row_off + S->levels[l].rows_pad) li = l;
+        if (li >= 0) {
+            const Level& L = S->levels[li];
+            const long long t0 = L.row_off / TC, ntl = L.rows_pad / TC;
+            const long long cc = std::min(std::max(row / TC, t0), t0 + ntl - 1);
+            std::vector<int> spiral;
+            spiral.push_back((int)cc);
+            for (long long dlt = 1; dlt < ntl; ++dlt) {
+                if (cc + dlt < t0 + ntl) spiral.push_back((int)(cc + dlt));
+                if (cc - dlt >= t0) spiral.push_back((int)(cc - dlt));
+            }
+            const int warm = (int)std::min<size_t>(kWarmTiles, spiral.size());
+            for (int w = 0; w < warm; ++w) J.push_back(Job{(int)t, spiral[w], 2, 0});
+            for (size_t w = 0; w < spiral.size(); ++w) J.push_back(Job{(int)t, spiral[w], (int)w < warm ? 4 : 0, 0});
         }
-        if (maxid < 0) continue;
-        long long cend = predecessor ? (maxid + TC - 1) / TC : nct;  // candidates < maxid
-        if (cend > nct) cend = nct;
-        for (long long c = 0; c < cend; ++c) jbv.push_back(Job{(int)t, (int)c, 0, 0});
+        if (predecessor) {
+            // ids >= the level size are not in the level: sweep them in dataset order
+            long long lo_tile = (li >= 0 && li < nlev - 1) ? S->levels[li].size / TC : (li == nlev - 1 ? n_ds_tiles : 0);
+            long long hi_tile = std::min((maxq + TC - 1) / TC, n_ds_tiles);
+            for (long long c = lo_tile; c < hi_tile; ++c) J.push_back(Job{(int)t, (int)c, 1, 0});
+        }
+        if (!J.empty()) J[0].first = 1;
     }
-    A((void**)&jobs_a, sizeof(Job) * (ja.size() + 1));
-    A((void**)&jobs_b, sizeof(Job) * (jbv.size() + 1));
-    if (e == cudaSuccess && !ja.empty()) e = cudaMemcpyAsync(jobs_a, ja.data(), sizeof(Job) * ja.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && !jbv.empty()) e = cudaMemcpyAsync(jobs_b, jbv.data(), sizeof(Job) * jbv.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * nq, st);
+    // longest-processing-time assignment of query tiles to persistent CTAs
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    std::vector<long long> order;
+    for (long long t = 0; t < nqt; ++t) if (!tiles[t].empty()) order.push_back(t);
+    std::sort(order.begin(), order.end(), [&](long long a, long long b) { return tiles[a].size() > tiles[b].size(); });
+    const int ncta = (int)std::min<long long>((long long)sms, (long long)order.size());
+    std::vector<std::vector<long long>> per_cta(ncta);
+    std::vector<std::pair<long long, int>> load;  // (jobs, cta) min-heap
+    for (int c = 0; c < ncta; ++c) load.push_back({0, c});
+    auto cmp = [](const std::pair<long long, int>& a, const std::pair<long long, int>& b) { return a.first > b.first; };
+    std::make_heap(load.begin(), load.end(), cmp);
+    for (long long t : order) {
+        std::pop_heap(load.begin(), load.end(), cmp);
+        auto& lc = load.back();
+        per_cta[lc.second].push_back(t);
+        lc.first += (long long)tiles[t].size();
+        std::push_heap(load.begin(), load.end(), cmp);
+    }
+    std::vector<Job> flat;
+    std::vector<int> begin(ncta + 1, 0);
+    for (int c = 0; c < ncta; ++c) {
+        begin[c] = (int)flat.size();
+        for (long long t : per_cta[c]) flat.insert(flat.end(), tiles[t].begin(), tiles[t].end());
+    }
+    begin[ncta] = (int)flat.size();
+    long long pairs_main = (long long)flat.size() * TQ * TC;
+    A((void**)&jobs, sizeof(Job) * (flat.size() + 1));
+    A((void**)&cta_begin, sizeof(int) * (ncta + 1));
+    if (e == cudaSuccess && !flat.empty()) e = cudaMemcpyAsync(jobs, flat.data(), sizeof(Job) * flat.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cta_begin, begin.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * 2 * nq, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(nfull_d, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(evals_d, 0, sizeof(long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(int), st);
-    const int wwidth = WINDOW_TILES * TC;
-    if (e == cudaSuccess) e = cudaMemsetAsync(win, 0x40, sizeof(float) * nq * wwidth, st);  // 0x40404040 ~ 3.0f: invalid
-    // ---- Pass A
+    // ---- sweep
+    if (timing) cudaEventRecord(ev[1], st);
+    if (timing) cudaEventRecord(ev[2], st);
     MMAParams P{};
-    P.b_hi = S->hil_hi; P.b_lo = S->hil_lo; P.b_groups = S->rows_pad / 8;
-    P.a_hi = Ah_hi; P.a_lo = Ah_lo; P.a_groups = gh;
-    P.m = m; P.jobs = jobs_a; P.njobs = (int)ja.size();
-    P.a_slot = a_slot_hil; P.slot_id = slot_id; P.b_id = S->b_id_hil;
+    P.a_hi = al_hi; P.a_lo = al_lo; P.a_groups = rows_q / 8;
+    P.b_hi[0] = S->lvl_hi; P.b_lo[0] = S->lvl_lo; P.b_groups[0] = S->lvl_rows / 8; P.b_id[0] = S->lvl_id;
+    P.b_hi[1] = S->ds_hi; P.b_lo[1] = S->ds_lo; P.b_groups[1] = S->rows_pad / 8; P.b_id[1] = S->b_id_ds;
+    P.m = m; P.jobs = jobs; P.cta_job_begin = cta_begin;
+    P.a_slot = a_slot_lvl; P.slot_id = slot_id;
     P.xs = xs; P.d = d; P.vn = S->vn; P.isp = S->isp; P.xmax = S->xmax;
     P.var = var; P.kernel_type = kernel_type; P.predecessor = predecessor ? 1 : 0;
-    P.err_coef = err_coef_for(m); P.mode = MODE_WINDOW; P.out_f = win; P.out_stride = wwidth;
-    P.tau2 = tau2; P.surv = surv; P.surv_cnt = surv_cnt; P.status = S->status;
-    if (e == cudaSuccess) e = launch_mma(P, st);
-    if (e == cudaSuccess) {
-        const int wpb = 4;
-        window_tau_kernel<<<(unsigned)((rows_q + wpb - 1) / wpb), 32 * wpb, sizeof(unsigned long long) * RBUF * wpb, st>>>(
-            win, wwidth, a_slot_hil, rows_q, k, tau2);
-        e = cudaGetLastError();
-    }
-    // ---- Pass B
-    P.b_hi = S->ds_hi; P.b_lo = S->ds_lo; P.b_groups = S->rows_pad / 8;
-    P.a_hi = Aq_hi; P.a_lo = Aq_lo; P.a_groups = gq;
-    P.jobs = jobs_b; P.njobs = (int)jbv.size(); P.a_slot = a_slot_ds; P.b_id = S->b_id_ds;
-    P.mode = MODE_FILTER;
-    if (e == cudaSuccess) e = launch_mma(P, st);
+    P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
+    P.surv = surv; P.surv_cnt = surv_cnt; P.status = S->status;
+    if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
+    if (timing) cudaEventRecord(ev[3], st);
     // ---- rescoring
     RescoreParams R{};
     R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls = S->inv_ls64; R.p = p;
@@ -837,6 +1023,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         rescore_kernel<<<(unsigned)((nq + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 0);
         collect_overflow_kernel<<<grid_for(nq), 256, 0, st>>>(surv_cnt, nq, full_list, nfull_d);
         e = cudaGetLastError();
+        launches += 2;
     }
     int nfull = 0, status = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nfull, nfull_d, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -846,27 +1033,45 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         R.nfull = nfull;
         rescore_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 1);
         e = cudaGetLastError();
+        ++launches;
     }
+    float ms_total = 0.f, ms_a = 0.f, ms_b = 0.f, ms_r = 0.f;
+    if (timing && e == cudaSuccess) {
+        cudaEventRecord(ev[4], st);
+        e = cudaEventSynchronize(ev[4]);
+        if (e == cudaSuccess) {
+            cudaEventElapsedTime(&ms_total, ev[0], ev[4]);
+            cudaEventElapsedTime(&ms_a, ev[0], ev[2]);
+            cudaEventElapsedTime(&ms_b, ev[2], ev[3]);
+            cudaEventElapsedTime(&ms_r, ev[3], ev[4]);
+        }
+    }
+    if (timing) for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
     long long evals = 0;
     if (e == cudaSuccess && stats) {
         e = cudaMemcpyAsync(&evals, evals_d, sizeof(long long), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
-    cudaFreeAsync(slot_id, st); cudaFreeAsync(val_ds, st); cudaFreeAsync(val_hil, st); cudaFreeAsync(vtmp, st);
-    cudaFreeAsync(key_ds, st); cudaFreeAsync(key_hil, st); cudaFreeAsync(ktmp, st); cudaFreeAsync(hist, st);
-    cudaFreeAsync(a_slot_ds, st); cudaFreeAsync(a_slot_hil, st); cudaFreeAsync(rowmap_ds, st); cudaFreeAsync(rowmap_hil, st);
-    if (aq_hi) { cudaFreeAsync(aq_hi, st); cudaFreeAsync(aq_lo, st); }
-    if (ah_hi) { cudaFreeAsync(ah_hi, st); cudaFreeAsync(ah_lo, st); }
-    cudaFreeAsync(win, st); cudaFreeAsync(tau2, st); cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
+    cudaFreeAsync(slot_id, st); cudaFreeAsync(val_lvl, st); cudaFreeAsync(vtmp, st);
+    cudaFreeAsync(key_lvl, st); cudaFreeAsync(ktmp, st); cudaFreeAsync(hist, st);
+    cudaFreeAsync(a_slot_lvl, st); cudaFreeAsync(rowmap_lvl, st);
+    cudaFreeAsync(al_hi, st); cudaFreeAsync(al_lo, st);
+    cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
-    cudaFreeAsync(jobs_a, st); cudaFreeAsync(jobs_b, st);
+    cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form: %s", cudaGetErrorString(e));
     if (status != 0) return set_err(CT_ERR_TIMEOUT, "screened form: pipeline wait timed out (code %d)", status);
     if (stats) {
-        stats->pairs_screened = (long long)(ja.size() + jbv.size()) * TQ * TC;
+        stats->pairs_screened = pairs_main;
         stats->pairs_rescored = evals;
         stats->distance_evals = evals;
-        stats->kernel_launches = 6 + (nfull > 0 ? 1 : 0);
+        stats->kernel_launches = launches;
+        stats->device_ms = ms_total;
+        stats->threshold_ms = ms_a;
+        stats->screen_ms = ms_b;
+        stats->rescore_ms = ms_r;
+        stats->screen_pairs_main = pairs_main;
+        stats->overflow_queries = nfull;
     }
     return CT_OK;
 }
@@ -877,28 +1082,32 @@ int ct_screen_debug_dots(ct_tree* T, const int* rows_a, const int* rows_b, float
     cudaError_t e = cudaSuccess;
     bf16 *ahi = nullptr, *alo = nullptr, *bhi = nullptr, *blo = nullptr;
     Job* job = nullptr;
-    int* status = nullptr;
+    int *status = nullptr, *begin = nullptr;
     const int m = T->m;
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes, st); };
     A((void**)&ahi, sizeof(bf16) * TQ * m); A((void**)&alo, sizeof(bf16) * TQ * m);
     A((void**)&bhi, sizeof(bf16) * TC * m); A((void**)&blo, sizeof(bf16) * TC * m);
-    A((void**)&job, sizeof(Job)); A((void**)&status, sizeof(int));
+    A((void**)&job, sizeof(Job)); A((void**)&status, sizeof(int)); A((void**)&begin, 2 * sizeof(int));
     if (e != cudaSuccess) return T->set_err(CT_ERR_NOMEM, "debug dots allocation: %s", cudaGetErrorString(e));
     split_blocked_kernel<<<64, 256, 0, st>>>(T->vnat, m, rows_a, TQ, ahi, alo);
     split_blocked_kernel<<<64, 256, 0, st>>>(T->vnat, m, rows_b, TC, bhi, blo);
-    Job hj{0, 0, 0, 0};
+    Job hj{0, 0, 0, 1};
+    int hb[2] = {0, 1};
     int zero = 0;
     e = cudaMemcpyAsync(job, &hj, sizeof(Job), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(begin, hb, sizeof(hb), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(status, &zero, sizeof(int), cudaMemcpyHostToDevice, st);
     MMAParams P{};
-    P.a_hi = ahi; P.a_lo = alo; P.a_groups = TQ / 8; P.b_hi = bhi; P.b_lo = blo; P.b_groups = TC / 8;
-    P.m = m; P.jobs = job; P.njobs = 1; P.mode = MODE_DEBUG; P.out_f = out; P.status = status;
-    if (e == cudaSuccess) e = launch_mma(P, st);
+    P.a_hi = ahi; P.a_lo = alo; P.a_groups = TQ / 8;
+    P.b_hi[0] = bhi; P.b_lo[0] = blo; P.b_groups[0] = TC / 8;
+    P.b_hi[1] = bhi; P.b_lo[1] = blo; P.b_groups[1] = TC / 8;
+    P.m = m; P.jobs = job; P.cta_job_begin = begin; P.k = 1; P.nstages = STAGES; P.out_f = out; P.status = status;
+    if (e == cudaSuccess) e = launch_sweep(P, MODE_DEBUG, 1, st);
     int hs = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     cudaFreeAsync(ahi, st); cudaFreeAsync(alo, st); cudaFreeAsync(bhi, st); cudaFreeAsync(blo, st);
-    cudaFreeAsync(job, st); cudaFreeAsync(status, st);
+    cudaFreeAsync(job, st); cudaFreeAsync(status, st); cudaFreeAsync(begin, st);
     if (e != cudaSuccess) return T->set_err(CT_ERR_CUDA, "debug dots: %s", cudaGetErrorString(e));
     if (hs != 0) return T->set_err(CT_ERR_TIMEOUT, "debug dots: pipeline wait timed out (code %d)", hs);
     return CT_OK;

@@ -68,15 +68,25 @@ extern "C" {
 typedef struct ct_tree ct_tree;
 
 typedef struct {
-    int64_t distance_evals;   /* residual distances evaluated (reference `distance_evals`) */
-    int64_t pairs_screened;   /* query x candidate pairs screened by the BF16 pass        */
-    int64_t pairs_rescored;   /* pairs rescored in compensated FP32 / FP64                */
-    int64_t kernel_launches;  /* engine kernels launched by the call                      */
-    double device_ms;         /* device time of the call (0 unless timing was requested)  */
+    int64_t distance_evals;   /* residual distances evaluated exactly (reference `distance_evals`) */
+    int64_t pairs_screened;   /* query x candidate pairs screened by the BF16 passes          */
+    int64_t pairs_rescored;   /* pairs rescored in compensated FP32 + FP64                    */
+    int64_t kernel_launches;  /* engine kernels launched by the call                          */
+    double device_ms;         /* device time of the whole call (timing enabled, else 0)       */
+    double screen_ms;         /* tensor-core screening kernel of the main sweep (Pass B)      */
+    double threshold_ms;      /* threshold pass (Pass A + k-th bound selection)               */
+    double rescore_ms;        /* rescoring kernels                                            */
+    int64_t screen_pairs_main;/* pairs screened by the main sweep                             */
+    int64_t overflow_queries; /* queries whose survivor list overflowed (rescored exhaustively) */
 } ct_stats;
 
 /* Library version (major*10000 + minor*100 + patch). */
 CT_API int ct_version(void);
+
+/* Per-phase device timing for the calling thread (0 = off, default).  When on, each
+ * ct_knn_residual records CUDA events around its kernels, synchronises its stream before
+ * returning and fills the *_ms fields of ct_stats.  No counterpart in the reference. */
+CT_API int ct_set_timing(int enable);
 
 /* Message of the calling thread's last failure ("" if none). */
 CT_API const char* ct_last_error(void);

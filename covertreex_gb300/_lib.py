@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = (
     "ct_last_error",
     "ct_build_residual",
     "ct_knn_residual",
+    "ct_knn_euclidean",
     "ct_tree_arrays",
     "ct_tree_shape",
     "ct_debug_screen_dots",
@@ -102,6 +103,8 @@ def load(build_if_missing: bool = True):
                                         i32, i32, u64, i32, vp, ctypes.POINTER(vp)]
         L.ct_knn_residual.restype = ctypes.c_int
         L.ct_knn_residual.argtypes = [vp, vp, i64, i32, i32, i32, vp, vp, ctypes.POINTER(CtStats), vp]
+        L.ct_knn_euclidean.restype = ctypes.c_int
+        L.ct_knn_euclidean.argtypes = [vp, i64, i32, vp, i64, i32, i32, vp, vp, vp]
         L.ct_tree_arrays.restype = ctypes.c_int
         L.ct_tree_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.ct_tree_shape.restype = ctypes.c_int

@@ -176,6 +176,19 @@ int ct_debug_screen_dots(ct_tree* T, const int32_t* rows_a, const int32_t* rows_
     return rc ? fail(rc, "ct_debug_screen_dots: %s", T->err) : CT_OK;
 }
 
+int ct_knn_euclidean(const float* points, int64_t n, int32_t d, const float* queries, int64_t nq, int32_t k,
+                     int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream) {
+    if (n < 0 || nq < 0) return fail(CT_ERR_ARG, "ct_knn_euclidean: negative size");
+    if (k <= 0) return fail(CT_ERR_ARG, "ct_knn_euclidean: k=%d must be positive", k);
+    if (k > ct::euclid_max_k()) return fail(CT_ERR_UNSUPPORTED, "ct_knn_euclidean: k=%d above %d", k, ct::euclid_max_k());
+    if (d <= 0 || d > ct::euclid_max_d()) return fail(CT_ERR_UNSUPPORTED, "ct_knn_euclidean: d=%d outside [1, %d]", d, ct::euclid_max_d());
+    if (nq == 0) return CT_OK;
+    if (!points || !queries || !out_idx || !out_dist) return fail(CT_ERR_ARG, "ct_knn_euclidean: NULL pointer");
+    CT_CUDA(ct::launch_euclid_knn(points, n, d, queries, nq, k, predecessor ? 1 : 0, (long long*)out_idx, out_dist,
+                                  (cudaStream_t)stream), "euclidean kNN launch");
+    return CT_OK;
+}
+
 int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {
     if (!T) return fail(CT_ERR_ARG, "ct_tree_shape: tree is NULL");
     if (n) *n = T->n;

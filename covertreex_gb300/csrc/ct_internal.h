@@ -39,4 +39,10 @@ cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long 
                              bool* result_in_tmp);
 int radix_num_blocks(long long n);
 
+// ct_euclid.cu
+cudaError_t launch_euclid_knn(const float* pts, long long n, int d, const float* qry, long long nq, int k,
+                              int predecessor, long long* out_idx, float* out_dist, cudaStream_t st);
+int euclid_max_k();
+int euclid_max_d();
+
 }  // namespace ct

@@ -268,7 +268,8 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     if (cid >= 0) {
 #pragma unroll
                         for (int c = 0; c < kMaxD; ++c) o[c] = c < P.d ? P.xs[(size_t)cid * P.d + c] : 0.f;
-                        o[8] = P.vn[cid]; o[9] = P.isp[cid]; o[10] = P.xmax[cid]; o[11] = __int_as_float(cid);
+                        o[8] = P.err_coef * P.vn[cid]; o[9] = P.isp[cid]; o[10] = 2.4e-7f * P.xmax[cid];
+                        o[11] = __int_as_float(cid);
                     } else {
 #pragma unroll
                         for (int c = 0; c < 11; ++c) o[c] = 0.f;
@@ -295,9 +296,13 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         unsigned gen = 0;  // query-tile generation, tags the shared row threshold
         float tau2 = 1.f;
         float xq[kMaxD];
-        float cq = 0.f, isq = 0.f, xmq = 0.f;
+        float vnq = 0.f, isq = 0.f, aq = 0.f;
+        // keep the pair iff (R + e) * isc >= thr_keep; it may enter the heap iff
+        // (R - e) * isc > thr_heap (both derived from tau2 / the heap top; see below)
+        float thr_keep = 0.f, thr_heap = 0.f;
 #pragma unroll
         for (int c = 0; c < kMaxD; ++c) xq[c] = 0.f;
+        const float dd = (float)P.d;
         for (int j = jb0; j < jb1; ++j, ++lt) {
             const Job jb = P.jobs[j];
             const int acc = lt & 1;
@@ -309,82 +314,92 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 qid = slot >= 0 ? P.slot_id[slot] : -1;
                 hn = 0; cnt = 0; tau2 = 1.f; ++gen;
                 if (qid >= 0) {
-                    cq = P.err_coef * P.vn[qid]; isq = P.isp[qid]; xmq = P.xmax[qid];
+                    vnq = P.vn[qid]; isq = P.isp[qid]; aq = 2.4e-7f * P.xmax[qid];
 #pragma unroll
                     for (int c = 0; c < kMaxD; ++c) xq[c] = c < P.d ? P.xs[(size_t)qid * P.d + c] : 0.f;
                 }
+                thr_keep = 0.f;   // tau2 = 1: keep everything
+                thr_heap = -CT_FLT_MAX;  // heap not full: every pair enters
             }
             if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) break;
             if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) break;
             sm::tc_fence_after();
             const float* rb = recs + (size_t)acc * TC * REC;
-            for (int cc = 0; cc < 4; ++cc) {
-                float v[32];
-                const int col0 = half * 128 + cc * 32;
-                sm::tmem_ld32(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TC + col0), v);
+            const bool keep_job = !(jb.which & 2);
+            const bool feed_heap = !(jb.which & 4);
+            if (MODE == MODE_SWEEP && qid >= 0) {
+                // the other half's threshold, when it belongs to this query tile
+                const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
+                if ((unsigned)(w >> 32) == gen) {
+                    const float t = __uint_as_float(~(unsigned)w);
+                    if (t < tau2) { tau2 = t; thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq; }
+                }
+            }
+            for (int cc = 0; cc < 16; ++cc) {
+                float v[8];
+                const int col0 = half * 128 + cc * 8;
+                sm::tmem_ld8(tmem_base + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * TC + col0), v);
                 if (MODE == MODE_DEBUG) {
                     float* o = P.out_f + ((size_t)(j - jb0) * TQ + row) * TC + col0;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) o[i] = v[i];
+                    for (int i = 0; i < 8; ++i) o[i] = v[i];
                     continue;
                 }
                 if (qid < 0) continue;
-                const bool keep = !(jb.which & 2);
-                {   // the other half's threshold, when it belongs to this query tile
-                    const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
-                    if ((unsigned)(w >> 32) == gen) tau2 = fminf(tau2, __uint_as_float(~(unsigned)w));
-                }
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
+                for (int i = 0; i < 8; ++i) {
                     const float4* r4 = (const float4*)(rb + (col0 + i) * REC);
-                    const float4 xa = r4[0], xb = r4[1], meta = r4[2];
+                    const float4 meta = r4[2];
                     const int cid = __float_as_int(meta.w);
                     if (cid < 0 || (P.predecessor && cid >= qid)) continue;
-                    float dl2 = 0.f, du2 = 0.f;
-                    if (cid != qid) {
-                        const float xc[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-                        float d2 = 0.f;
+                    const float4 xa = r4[0], xb = r4[1];
+                    const float xc[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+                    float d2 = 0.f;
 #pragma unroll
-                        for (int c = 0; c < kMaxD; ++c) { float t = xq[c] - xc[c]; d2 = fmaf(t, t, d2); }
-                        // error of d2: rounding of the sum and of the scaled coordinates
-                        const float ed2 = (float)(P.d + 2) * 5.97e-8f * d2 +
-                                          4.8e-7f * sqrtf((float)P.d * d2) * (xmq + meta.z);
-                        float kv, ek;
-                        if (P.kernel_type == 0) {
-                            const float x = -0.5f * d2;
-                            kv = P.var * __expf(x);
-                            ek = kv * (1e-6f + 1.2e-7f * fabsf(x) + 0.5f * ed2);
-                        } else {
-                            const float a = 2.2360679775f * sqrtf(d2);
-                            const float ea = __expf(-a);
-                            kv = P.var * (1.f + a + a * a * 0.33333334f) * ea;
-                            ek = kv * (1e-6f + 2.4e-7f * a) + P.var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
-                        }
-                        const float R = fabsf(kv - v[i]);
-                        const float e = cq * meta.x + ek + R * 1.2e-7f + 1e-30f;
-                        const float sc = isq * meta.y;
-                        dl2 = 1.f - fminf((R + e) * sc * (1.f + 1e-6f), 1.f);
-                        du2 = 1.f - fminf(fmaxf(R - e, 0.f) * sc * (1.f - 1e-6f), 1.f);
+                    for (int c = 0; c < kMaxD; ++c) { const float t = xq[c] - xc[c]; d2 = fmaf(t, t, d2); }
+                    // Certified error of the kernel value.  d2 error: (D+2) 2^-24 d2 from the
+                    // sum plus 2^-22 sum|dx| (|x_q| + |x_c|) from the scaled coordinates, with
+                    // sum|dx| <= sqrt(D d2) <= (D d2 + 1) / 2.
+                    const float axm = aq + meta.z;                      // 2.4e-7 (|x_q| + |x_c|)
+                    const float ed2 = fmaf((dd + 2.f) * 5.97e-8f, d2, 0.5f * axm * fmaf(dd, d2, 1.f));
+                    float kv, ek;
+                    if (P.kernel_type == 0) {
+                        kv = P.var * __expf(-0.5f * d2);
+                        ek = kv * fmaf(6e-8f, d2, fmaf(0.5f, ed2, 1e-6f));
+                    } else {
+                        const float a = 2.2360679775f * sqrtf(d2);
+                        const float ea = __expf(-a);
+                        kv = P.var * (1.f + a + a * a * 0.33333334f) * ea;
+                        ek = kv * (1e-6f + 2.4e-7f * a) + P.var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
                     }
-                    if (keep && dl2 <= tau2) {
+                    const float R = fabsf(kv - v[i]);
+                    const float e = fmaf(vnq, meta.x, ek) + fmaf(R, 1.2e-7f, 1e-30f);
+                    const bool self = cid == qid;
+                    if (keep_job && (self || (R + e) * meta.y >= thr_keep)) {
                         if (cnt < HALF_CAP) P.surv[((size_t)slot * 2 + half) * HALF_CAP + cnt] = cid;
                         ++cnt;
                     }
-                    // running k smallest upper bounds of this row half -> tau2.  Warm-up
-                    // jobs repeat later as kept jobs, so they only feed the heap once.
-                    if (!keep || !jb_warm_seen(jb)) {
+                    if (feed_heap && (self || (R - e) * meta.y > thr_heap)) {
+                        // exact certified upper bound of d^2 for this pair
+                        const float du2 = self ? 0.f
+                                               : 1.f - fminf(fmaxf(R - e, 0.f) * (isq * meta.y) * (1.f - 1e-6f), 1.f);
+                        bool changed = false;
                         if (hn < P.k) {
                             heap_push(heap, hn, du2);
                             ++hn;
-                            if (hn == P.k && heap[0] < tau2) {
-                                tau2 = heap[0];
-                                atomicMax(&rowtau[row], ((unsigned long long)gen << 32) | (unsigned long long)(~__float_as_uint(tau2)));
-                            }
+                            changed = hn == P.k;
                         } else if (du2 < heap[0]) {
                             heap_sift_down(heap, hn, du2);
-                            if (heap[0] < tau2) {
-                                tau2 = heap[0];
-                                atomicMax(&rowtau[row], ((unsigned long long)gen << 32) | (unsigned long long)(~__float_as_uint(tau2)));
+                            changed = true;
+                        }
+                        if (changed) {
+                            const float top = heap[0];
+                            thr_heap = (1.f - top) * (1.f + 2e-6f) / isq;
+                            if (top < tau2) {
+                                tau2 = top;
+                                thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq;
+                                atomicMax(&rowtau[row], ((unsigned long long)gen << 32) |
+                                                            (unsigned long long)(~__float_as_uint(tau2)));
                             }
                         }
                     }
@@ -610,6 +625,94 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
         P.out_dist[(size_t)slot * k + j] = ok ? __uint_as_float((unsigned)(key >> 32)) : CT_FLT_MAX;
     }
     if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
+}
+
+// Exhaustive rescoring of overflowed queries, split for parallelism: each warp
+// scores one chunk of a query's candidate range and keeps its k best keys.
+constexpr int kChunk = 4096;
+struct ChunkItem {
+    int slot, chunk;
+};
+
+__device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& fill, int k, bool has,
+                                                 unsigned long long key) {
+    const int lane = threadIdx.x & 31;
+    unsigned mask = __ballot_sync(0xffffffffu, has);
+    int added = __popc(mask);
+    if (fill + added > RBUF) {
+        __syncwarp();
+        warp_bitonic_sort(keys);
+        for (int i = k + lane; i < RBUF; i += 32) keys[i] = ~0ULL;
+        __syncwarp();
+        fill = k;
+    }
+    if (has) keys[fill + __popc(mask & ((1u << lane) - 1u))] = key;
+    fill += added;
+    __syncwarp();
+}
+
+__global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, int nitems,
+                                     unsigned long long* partial) {
+    extern __shared__ unsigned long long ckeys_all[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x / 32;
+    unsigned long long* keys = ckeys_all + (size_t)warp * RBUF;
+    const long long w = (long long)blockIdx.x * wpb + warp;
+    if (w >= nitems) return;
+    const ChunkItem it = items[w];
+    const int q = P.slot_id[it.slot];
+    const int k = P.k;
+    float vql[32];
+#pragma unroll
+    for (int t = 0; t < 32; ++t) vql[t] = (t * 32 + lane < P.m) ? P.v[(size_t)q * P.m + t * 32 + lane] : 0.f;
+    for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
+    __syncwarp();
+    const long long count = P.predecessor ? (long long)q : P.n;
+    const long long b0 = (long long)it.chunk * kChunk;
+    const long long b1 = b0 + kChunk < count ? b0 + kChunk : count;
+    int fill = k;
+    for (long long base = b0; base < b1; base += 32) {
+        const int nb = (int)((b1 - base) < 32 ? (b1 - base) : 32);
+        const int cid = lane < nb ? (int)(base + lane) : -1;
+        double mydot = 0.0;
+        for (int t = 0; t < nb; ++t) {
+            const double dot = warp_dot_compensated(P, (int)(base + t), vql);
+            if (lane == t) mydot = dot;
+        }
+        const float dist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
+        warp_topk_append(keys, fill, k, lane < nb, pack_key(dist, cid));
+    }
+    warp_bitonic_sort(keys);
+    for (int j = lane; j < k; j += 32) partial[(size_t)w * k + j] = keys[j];
+    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)(b1 - b0));
+}
+
+// Merge the chunk results of each overflowed query into its output row.
+__global__ void merge_chunks_kernel(RescoreParams P, const int* item_begin, const unsigned long long* partial) {
+    extern __shared__ unsigned long long mkeys_all[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x / 32;
+    unsigned long long* keys = mkeys_all + (size_t)warp * RBUF;
+    const long long w = (long long)blockIdx.x * wpb + warp;
+    if (w >= P.nfull) return;
+    const int slot = P.full_slots[w];
+    const int k = P.k;
+    for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
+    __syncwarp();
+    int fill = k;
+    const long long e0 = (long long)item_begin[w] * k, e1 = (long long)item_begin[w + 1] * k;
+    for (long long base = e0; base < e1; base += 32) {
+        const bool has = base + lane < e1;
+        const unsigned long long key = has ? partial[base + lane] : ~0ULL;
+        warp_topk_append(keys, fill, k, has && key != ~0ULL, key);
+    }
+    warp_bitonic_sort(keys);
+    for (int j = lane; j < k; j += 32) {
+        const unsigned long long key = keys[j];
+        const bool ok = key != ~0ULL;
+        P.out_idx[(size_t)slot * k + j] = ok ? (long long)(unsigned)(key & 0xffffffffULL) : -1LL;
+        P.out_dist[(size_t)slot * k + j] = ok ? __uint_as_float((unsigned)(key >> 32)) : CT_FLT_MAX;
+    }
 }
 
 __global__ void collect_overflow_kernel(const int* __restrict__ surv_cnt, long long nslots, int* __restrict__ list,
@@ -1029,11 +1132,42 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nfull, nfull_d, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, S->status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    ChunkItem* items_d = nullptr;
+    int* item_begin_d = nullptr;
+    unsigned long long* partial = nullptr;
     if (e == cudaSuccess && nfull > 0) {
+        // split every overflowed query's exhaustive range into chunks
+        std::vector<int> fl(nfull), sid(nq);
+        e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id, sizeof(int) * nq, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        std::sort(fl.begin(), fl.end());
+        std::vector<ChunkItem> items;
+        std::vector<int> ibeg(nfull + 1, 0);
+        for (int i = 0; i < nfull; ++i) {
+            ibeg[i] = (int)items.size();
+            const long long count = predecessor ? (long long)sid[fl[i]] : n;
+            for (long long c = 0; c * kChunk < count; ++c) items.push_back(ChunkItem{fl[i], (int)c});
+        }
+        ibeg[nfull] = (int)items.size();
+        const int nitems = (int)items.size();
+        A((void**)&items_d, sizeof(ChunkItem) * (nitems + 1));
+        A((void**)&item_begin_d, sizeof(int) * (nfull + 1));
+        A((void**)&partial, sizeof(unsigned long long) * ((size_t)nitems * k + 1));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(items_d, items.data(), sizeof(ChunkItem) * nitems, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, st);
         R.nfull = nfull;
-        rescore_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 1);
-        e = cudaGetLastError();
-        ++launches;
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(merge_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        if (e == cudaSuccess && nitems > 0) {
+            rescore_chunk_kernel<<<(unsigned)((nitems + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, items_d, nitems, partial);
+            merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, item_begin_d, partial);
+            e = cudaGetLastError();
+            launches += 2;
+        }
+        // (host vectors stay alive until the synchronisation below)
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
     float ms_total = 0.f, ms_a = 0.f, ms_b = 0.f, ms_r = 0.f;
     if (timing && e == cudaSuccess) {
@@ -1059,6 +1193,9 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
     cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st);
+    if (items_d) cudaFreeAsync(items_d, st);
+    if (item_begin_d) cudaFreeAsync(item_begin_d, st);
+    if (partial) cudaFreeAsync(partial, st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form: %s", cudaGetErrorString(e));
     if (status != 0) return set_err(CT_ERR_TIMEOUT, "screened form: pipeline wait timed out (code %d)", status);
     if (stats) {

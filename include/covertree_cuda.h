@@ -115,6 +115,15 @@ CT_API int ct_build_residual(const float* v, const float* p, const float* coords
 CT_API int ct_knn_residual(ct_tree* tree, const int64_t* q_ids, int64_t nq, int32_t k, int32_t predecessor, int32_t form,
                     int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream);
 
+/*
+ * Exact Euclidean kNN of `queries` [nq x d] against `points` [n x d] (device f32).
+ * Replaces CoverTreeWrapper.insert + knn_query for the Euclidean metric
+ * (src/lib.rs:207-223, 299-326; src/algo.rs:179-323).  predecessor != 0: query row i
+ * only gets points j < i (src/algo.rs:193-195).  d <= 16, k <= 64.
+ */
+CT_API int ct_knn_euclidean(const float* points, int64_t n, int32_t d, const float* queries, int64_t nq, int32_t k,
+                            int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream);
+
 /* Copy tree arrays to device buffers of n entries each (any may be NULL):
  * parents (node numbering), levels, si (cover radii), node_to_dataset, subtree_min. */
 CT_API int ct_tree_arrays(const ct_tree* tree, int64_t* parents, int32_t* levels, float* si, int64_t* node_to_dataset,

@@ -140,6 +140,8 @@ __global__ void __launch_bounds__(kThreads, 1) brute_knn_kernel(BruteParams P) {
     for (int qi = tid; qi < QT; qi += kThreads) {
         long long g = q0 + qi;
         long long id = g < P.nq ? P.qids[g] : -1;
+        if (id >= P.n) id = -1;  // ids outside [0, n) give an all-padding row
+        if (id < 0) id = -1;
         Qid[qi] = id;
         Cnt[qi] = 0;
         Nq[qi] = id >= 0 ? P.norms[id] : 0.f;

@@ -28,6 +28,7 @@ CT_FORM_DENSE = 0
 CT_FORM_TREE = 1
 CT_FORM_SCREENED = 2
 CT_BUILD_METRIC_ONLY = 1
+CT_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 FORMS = {"dense": CT_FORM_DENSE, "tree": CT_FORM_TREE, "screened": CT_FORM_SCREENED}
 
@@ -39,6 +40,7 @@ EXPORTED_SYMBOLS = (
     "ct_build_residual",
     "ct_knn_residual",
     "ct_knn_euclidean",
+    "ct_knn_residual_dense_noalloc",
     "ct_tree_arrays",
     "ct_tree_shape",
     "ct_debug_screen_dots",
@@ -105,6 +107,9 @@ def load(build_if_missing: bool = True):
         L.ct_knn_residual.argtypes = [vp, vp, i64, i32, i32, i32, vp, vp, ctypes.POINTER(CtStats), vp]
         L.ct_knn_euclidean.restype = ctypes.c_int
         L.ct_knn_euclidean.argtypes = [vp, i64, i32, vp, i64, i32, i32, vp, vp, vp]
+        L.ct_knn_residual_dense_noalloc.restype = ctypes.c_int
+        L.ct_knn_residual_dense_noalloc.argtypes = [vp, vp, vp, i64, i32, i32, f32, ctypes.POINTER(ctypes.c_float),
+                                                    i32, i32, vp, i64, i32, i32, vp, vp, vp]
         L.ct_tree_arrays.restype = ctypes.c_int
         L.ct_tree_arrays.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         L.ct_tree_shape.restype = ctypes.c_int

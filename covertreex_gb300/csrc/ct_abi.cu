@@ -15,6 +15,10 @@
 #include "ct_tree.h"
 
 int ct_screen_debug_dots(ct_tree* T, const int* rows_a, const int* rows_b, float* out, cudaStream_t st);
+int ct_noalloc_dense_impl(const float* v, const float* p, const float* coords, long long n, int m, int d,
+                          float variance, const float* lengthscale, int n_lengthscale, int kernel_type,
+                          const long long* q_ids, long long nq, int k, int predecessor, long long* out_idx,
+                          float* out_dist, cudaStream_t st, char* err, size_t errlen);
 
 namespace {
 
@@ -187,6 +191,24 @@ int ct_knn_euclidean(const float* points, int64_t n, int32_t d, const float* que
     CT_CUDA(ct::launch_euclid_knn(points, n, d, queries, nq, k, predecessor ? 1 : 0, (long long*)out_idx, out_dist,
                                   (cudaStream_t)stream), "euclidean kNN launch");
     return CT_OK;
+}
+
+int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* coords, int64_t n, int32_t m,
+                                  int32_t d, float variance, const float* lengthscale, int32_t n_lengthscale,
+                                  int32_t kernel_type, const int64_t* q_ids, int64_t nq, int32_t k,
+                                  int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream) {
+    if (n <= 0 || n >= (1LL << 31)) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: n=%lld outside [1, 2^31)", (long long)n);
+    if (m <= 0 || (m % 16) != 0) return fail(CT_ERR_UNSUPPORTED, "ct_knn_residual_dense_noalloc: m=%d must be a positive multiple of 16", m);
+    if (d <= 0 || d > 64) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: d=%d outside [1, 64]", d);
+    if (k <= 0 || k > 128) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: k=%d outside [1, 128]", k);
+    if (nq < 0) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: nq < 0");
+    if (!v || !p || !coords) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: NULL input pointer");
+    if (nq > 0 && (!q_ids || !out_idx || !out_dist)) return fail(CT_ERR_ARG, "ct_knn_residual_dense_noalloc: NULL pointer");
+    char msg[400];
+    int rc = ct_noalloc_dense_impl(v, p, coords, n, m, d, variance, lengthscale, n_lengthscale, kernel_type,
+                                   (const long long*)q_ids, nq, k, predecessor, (long long*)out_idx, out_dist,
+                                   (cudaStream_t)stream, msg, sizeof(msg));
+    return rc == CT_OK ? CT_OK : fail(rc, "ct_knn_residual_dense_noalloc: %s", msg);
 }
 
 int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {

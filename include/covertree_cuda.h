@@ -124,6 +124,28 @@ CT_API int ct_knn_residual(ct_tree* tree, const int64_t* q_ids, int64_t nq, int3
 CT_API int ct_knn_euclidean(const float* points, int64_t n, int32_t d, const float* queries, int64_t nq, int32_t k,
                             int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream);
 
+/*
+ * Allocation-free dense residual kNN.  No counterpart in the reference: for callers that
+ * cannot allocate device memory (their framework owns all GPU memory through its own
+ * pool, or their loop cannot afford the device synchronisation of cudaMalloc/cudaFree).
+ * Same result as ct_build_residual + ct_knn_residual(..., CT_FORM_DENSE, ...), bit for
+ * bit, from the caller's raw inputs (v [n x m], p [n], coords [n x d], q_ids [nq]; device)
+ * into the caller's outputs (out_idx [nq x k] int64, out_dist [nq x k] f32; device).
+ * lengthscale is a HOST pointer, as in ct_build_residual.
+ * Scratch: one fixed __device__ array of CT_NOALLOC_SCRATCH_BYTES (64 MiB) inside the
+ * library, held by every GPU that loads it until the process exits; a call needs
+ * 4 n (m + d + 2) bytes (256-byte aligned pieces) and is rejected with CT_ERR_UNSUPPORTED
+ * beyond that.  The first call on a device looks up the array's device address.  All
+ * calls share the array: calls whose GPU work overlaps (different streams, threads or
+ * processes' contexts on the same device) race and must be serialised by the caller.
+ * m must be a multiple of 16; k <= 128.  Allocates nothing.
+ */
+#define CT_NOALLOC_SCRATCH_BYTES (64ull << 20)
+CT_API int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* coords, int64_t n, int32_t m,
+                                         int32_t d, float variance, const float* lengthscale, int32_t n_lengthscale,
+                                         int32_t kernel_type, const int64_t* q_ids, int64_t nq, int32_t k,
+                                         int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream);
+
 /* Copy tree arrays to device buffers of n entries each (any may be NULL):
  * parents (node numbering), levels, si (cover radii), node_to_dataset, subtree_min. */
 CT_API int ct_tree_arrays(const ct_tree* tree, int64_t* parents, int32_t* levels, float* si, int64_t* node_to_dataset,

@@ -46,6 +46,7 @@ def parse_args():
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP32 form (0 = skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=2048, help="queries per CPU baseline sample")
+    ap.add_argument("--n", type=int, default=None, help="override N of the workload (profiling on a smaller case)")
     return ap.parse_args()
 
 
@@ -194,7 +195,7 @@ def main():
             import subprocess as sp
 
             sp.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-            wl = synthetic.make(args.workload)
+            wl = synthetic.make(args.workload, n=args.n)
             run_reference(args, wl)
         return
 
@@ -207,7 +208,7 @@ def main():
 
     _build.build_library()
     L = _lib.load()
-    wl = synthetic.make(args.workload)
+    wl = synthetic.make(args.workload, n=args.n)
     dev = torch.device("cuda", local)
     index = CudaResidualIndex(wl.v, wl.p, wl.coords, variance=wl.variance, lengthscale=[wl.lengthscale] * wl.d,
                               kernel_type=wl.kernel_type, build_tree=False, device=dev)

@@ -501,31 +501,76 @@ struct RescoreParams {
     long long* evals;
 };
 
-// Compensated FP32 dot product v_q . v_c (TwoProd via FMA, TwoSum), reduced
-// across the warp in FP64.  The warp holds the query row as vq[t] = v_q[32 t + lane]
-// (m <= 1024).  Every lane returns the full sum.
-__device__ __forceinline__ double warp_dot_compensated(const RescoreParams& P, int c, const float (&vq)[32]) {
-    const int lane = threadIdx.x & 31;
-    float s = 0.f, comp = 0.f;
-    const float* vc = P.v + (size_t)c * P.m;
+// Compensated FP32 dot product pieces (TwoProd via FMA, TwoSum).  The warp
+// splits a row of m <= 1024 floats into 32 lane slices of m/32 contiguous
+// elements (4-float aligned when m % 128 == 0, else scalar); each lane keeps
+// the query slice in registers and accumulates a (sum, compensation) pair.
+__device__ __forceinline__ void two_sum_acc(float& s, float& comp, float a, float b) {
+    const float pr = a * b;
+    const float pe = fmaf(a, b, -pr);
+    const float ts = s + pr;
+    const float z = ts - s;
+    const float se = (s - (ts - z)) + (pr - z);
+    s = ts;
+    comp += se + pe;
+}
+
+__device__ __forceinline__ double warp_sum_double(double v) {
 #pragma unroll
-    for (int t = 0; t < 32; ++t) {
-        const int e = t * 32 + lane;
-        if (e < P.m) {
-            float a = vq[t], b = __ldg(vc + e);
-            float pr = a * b;
-            float pe = fmaf(a, b, -pr);
-            float ts = s + pr;
-            float z = ts - s;
-            float se = (s - (ts - z)) + (pr - z);
-            s = ts;
-            comp += se + pe;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Load the query slice: lane l holds elements [l*m/32, (l+1)*m/32).
+__device__ __forceinline__ void load_query_slice(const float* row, int m, float (&vq)[32]) {
+    const int lane = threadIdx.x & 31;
+    const int per = m >> 5;
+    const float* r = row + (size_t)lane * per;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) vq[t] = t < per ? r[t] : 0.f;
+}
+
+// Dots of the query slice with NC candidate rows at once (independent loads in flight).
+template <int NC>
+__device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, const int (&cid)[NC],
+                                          const float (&vq)[32], double (&out)[NC]) {
+    const int lane = threadIdx.x & 31;
+    const int per = m >> 5;
+    float s[NC], comp[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) { s[c] = 0.f; comp[c] = 0.f; }
+    if ((per & 3) == 0) {
+#pragma unroll
+        for (int t4 = 0; t4 < 8; ++t4) {
+            if (t4 * 4 < per) {
+                float4 x[NC];
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+                    x[c] = cid[c] >= 0 ? __ldg((const float4*)(V + (size_t)cid[c] * m + (size_t)lane * per) + t4)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    two_sum_acc(s[c], comp[c], vq[4 * t4 + 0], x[c].x);
+                    two_sum_acc(s[c], comp[c], vq[4 * t4 + 1], x[c].y);
+                    two_sum_acc(s[c], comp[c], vq[4 * t4 + 2], x[c].z);
+                    two_sum_acc(s[c], comp[c], vq[4 * t4 + 3], x[c].w);
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+            if (t < per) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const float b = cid[c] >= 0 ? __ldg(V + (size_t)cid[c] * m + (size_t)lane * per + t) : 0.f;
+                    two_sum_acc(s[c], comp[c], vq[t], b);
+                }
+            }
         }
     }
-    double dot = (double)s + (double)comp;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, off);
-    return dot;
+    for (int c = 0; c < NC; ++c) out[c] = warp_sum_double((double)s[c] + (double)comp[c]);
 }
 
 // FP64 kernel value, normalisation and square root for one pair (one lane).
@@ -551,6 +596,9 @@ __device__ __forceinline__ float exact_from_dot(const RescoreParams& P, int q, i
     return (float)(ds > 0.0 ? sqrt(ds) : 0.0);
 }
 
+__device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& fill, int k, bool has,
+                                                 unsigned long long key);
+
 // One warp per query slot.  Candidates: the survivor list, or the full range
 // [0, limit) for slots listed in full_slots.  Streaming top-k through a sorted
 // shared buffer: entries [0, k) hold the current best, new candidates fill the
@@ -573,17 +621,15 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
         return;
     }
     const int k = P.k;
-    // query row slice held per lane
     float vql[32];
-#pragma unroll
-    for (int t = 0; t < 32; ++t) vql[t] = (t * 32 + lane < P.m) ? P.v[(size_t)q * P.m + t * 32 + lane] : 0.f;
+    load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
     for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
     __syncwarp();
     long long count = use_full ? (P.predecessor ? (long long)q : P.n) : (long long)(c0 + c1);
     int fill = k;  // next free position in the buffer
     long long evals = 0;
     for (long long base = 0; base < count; base += 32) {
-        // each lane fetches one candidate id; the warp scores them one at a time
+        // each lane fetches one candidate id; the warp scores them four at a time
         long long ci = base + lane;
         int cid = -1;
         if (ci < count)
@@ -592,30 +638,22 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
                                       : P.surv[(size_t)(2 * slot + 1) * HALF_CAP + (ci - c0)]);
         double mydot = 0.0;
         const int nb = (int)((count - base) < 32 ? (count - base) : 32);
-        for (int t = 0; t < nb; ++t) {
-            int c = __shfl_sync(0xffffffffu, cid, t);
-            double dot = warp_dot_compensated(P, c, vql);
-            if (lane == t) mydot = dot;
+        for (int t = 0; t < nb; t += 4) {
+            int cc[4];
+            double dots[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int src = __shfl_sync(0xffffffffu, cid, (t + u) & 31);
+                cc[u] = (t + u) < nb ? src : -1;
+            }
+            warp_dots<4>(P.v, P.m, cc, vql, dots);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (lane == t + u) mydot = dots[u];
         }
         float mydist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
         evals += nb;
-        // append to buffer
-        bool has = ci < count;
-        unsigned mask = __ballot_sync(0xffffffffu, has);
-        int pos = fill + __popc(mask & ((1u << lane) - 1u));
-        int added = __popc(mask);
-        if (fill + added > RBUF) {
-            // flush: sort and keep the best k, then append
-            __syncwarp();
-            warp_bitonic_sort(keys);
-            for (int i = k + lane; i < RBUF; i += 32) keys[i] = ~0ULL;
-            __syncwarp();
-            fill = k;
-            pos = fill + __popc(mask & ((1u << lane) - 1u));
-        }
-        if (has) keys[pos] = pack_key(mydist, cid);
-        fill += added;
-        __syncwarp();
+        warp_topk_append(keys, fill, k, ci < count, pack_key(mydist, cid));
     }
     warp_bitonic_sort(keys);
     for (int j = lane; j < k; j += 32) {
@@ -663,8 +701,7 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, in
     const int q = P.slot_id[it.slot];
     const int k = P.k;
     float vql[32];
-#pragma unroll
-    for (int t = 0; t < 32; ++t) vql[t] = (t * 32 + lane < P.m) ? P.v[(size_t)q * P.m + t * 32 + lane] : 0.f;
+    load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
     for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
     __syncwarp();
     const long long count = P.predecessor ? (long long)q : P.n;
@@ -675,9 +712,15 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, in
         const int nb = (int)((b1 - base) < 32 ? (b1 - base) : 32);
         const int cid = lane < nb ? (int)(base + lane) : -1;
         double mydot = 0.0;
-        for (int t = 0; t < nb; ++t) {
-            const double dot = warp_dot_compensated(P, (int)(base + t), vql);
-            if (lane == t) mydot = dot;
+        for (int t = 0; t < nb; t += 4) {
+            int cc[4];
+            double dots[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) cc[u] = (t + u) < nb ? (int)(base + t + u) : -1;
+            warp_dots<4>(P.v, P.m, cc, vql, dots);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (lane == t + u) mydot = dots[u];
         }
         const float dist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
         warp_topk_append(keys, fill, k, lane < nb, pack_key(dist, cid));

@@ -34,5 +34,5 @@ ct_tree::~ct_tree() {
     dfree(vperm); dfree(xs); dfree(norms); dfree(p); dfree(inv_ls); dfree(vnat); dfree(coords_raw);
     dfree(order); dfree(inv); dfree(parents); dfree(levels); dfree(si); dfree(sub_min);
     dfree(child_off); dfree(child_idx); dfree(roots);
-    dfree(tvperm); dfree(txs); dfree(tnorms); dfree(tp);
+    dfree(tvnat); dfree(txs); dfree(tnorms); dfree(tp);
 }

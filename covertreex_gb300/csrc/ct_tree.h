@@ -28,17 +28,17 @@ struct ct_tree {
 
     // cover tree (node order = build order; node i holds dataset row order[i])
     bool has_tree = false;
-    int64_t* order = nullptr;     // node -> dataset
-    int64_t* inv = nullptr;       // dataset -> node
-    int64_t* parents = nullptr;   // node numbering, -1 for roots
+    long long* order = nullptr;     // node -> dataset
+    long long* inv = nullptr;       // dataset -> node
+    long long* parents = nullptr;   // node numbering, -1 for roots
     int32_t* levels = nullptr;
     float* si = nullptr;          // cover radius (max distance to any descendant, upper bound)
-    int64_t* sub_min = nullptr;   // min dataset id in the subtree (node itself included)
-    int64_t* child_off = nullptr; // CSR children: child_off[n+1], child_idx[n]
-    int64_t* child_idx = nullptr;
-    int64_t* roots = nullptr;     // root nodes
+    long long* sub_min = nullptr;   // min dataset id in the subtree (node itself included)
+    long long* child_off = nullptr; // CSR children: child_off[n+1], child_idx[n]
+    long long* child_idx = nullptr;
+    long long* roots = nullptr;     // root nodes
     int64_t n_roots = 0;
-    float* tvperm = nullptr;      // tree-order copies for the traversal (residue-major V)
+    float* tvnat = nullptr;       // node-order copies for the build and traversal (natural-layout V)
     float* txs = nullptr;
     float* tnorms = nullptr;
     float* tp = nullptr;

@@ -45,6 +45,10 @@ EXPORTED_SYMBOLS = (
     "ct_tree_shape",
     "ct_debug_screen_dots",
     "ct_free",
+    "ct_vfactor_create",
+    "ct_vfactor_embed",
+    "ct_vfactor_chol",
+    "ct_vfactor_free",
 )
 
 
@@ -118,6 +122,15 @@ def load(build_if_missing: bool = True):
         L.ct_debug_screen_dots.argtypes = [vp, vp, vp, vp, vp]
         L.ct_free.restype = ctypes.c_int
         L.ct_free.argtypes = [vp]
+        f64 = ctypes.c_double
+        L.ct_vfactor_create.restype = ctypes.c_int
+        L.ct_vfactor_create.argtypes = [vp, i32, i32, i32, f64, f64, vp, ctypes.POINTER(vp)]
+        L.ct_vfactor_embed.restype = ctypes.c_int
+        L.ct_vfactor_embed.argtypes = [vp, vp, i64, vp, vp, vp]
+        L.ct_vfactor_chol.restype = ctypes.c_int
+        L.ct_vfactor_chol.argtypes = [vp, vp, vp]
+        L.ct_vfactor_free.restype = ctypes.c_int
+        L.ct_vfactor_free.argtypes = [vp]
         _handle = L
         return L
 

@@ -13,6 +13,7 @@
 #include "ct_common.cuh"
 #include "ct_internal.h"
 #include "ct_tree.h"
+#include "ct_vmatrix.h"
 
 int ct_screen_debug_dots(ct_tree* T, const int* rows_a, const int* rows_b, float* out, cudaStream_t st);
 int ct_noalloc_dense_impl(const float* v, const float* p, const float* coords, long long n, int m, int d,
@@ -222,6 +223,82 @@ int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {
 int ct_free(ct_tree* T) {
     if (!T) return CT_OK;
     delete T;
+    return CT_OK;
+}
+
+int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type, double variance,
+                      double lengthscale, void* stream, ct_vfactor** out) {
+    if (!out) return fail(CT_ERR_ARG, "ct_vfactor_create: out is NULL");
+    *out = nullptr;
+    if (m <= 0 || m > 16384) return fail(CT_ERR_ARG, "ct_vfactor_create: m=%d outside [1, 16384]", m);
+    if (d <= 0 || d > 64) return fail(CT_ERR_ARG, "ct_vfactor_create: d=%d outside [1, 64]", d);
+    if (!z) return fail(CT_ERR_ARG, "ct_vfactor_create: z is NULL");
+    if (kernel_type != CT_KERNEL_RBF && kernel_type != CT_KERNEL_MATERN52) kernel_type = CT_KERNEL_RBF;
+    cudaStream_t st = (cudaStream_t)stream;
+    ct_vfactor* F = new (std::nothrow) ct_vfactor();
+    if (!F) return fail(CT_ERR_NOMEM, "ct_vfactor_create: host allocation failed");
+    F->m = m; F->d = d; F->kernel_type = kernel_type; F->variance = variance; F->lengthscale = lengthscale;
+    cudaGetDevice(&F->device);
+    const size_t mm = (size_t)m * m;
+    int* status = nullptr;
+    int hs = 0;
+    cudaError_t e = cudaMalloc((void**)&F->z, sizeof(double) * (size_t)m * d);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&F->L, sizeof(double) * mm);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&F->Li, sizeof(double) * mm);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(F->z, z, sizeof(double) * (size_t)m * d, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = ct::vmatrix_factor(F->z, m, d, kernel_type, variance, lengthscale, F->L, F->Li, status, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (status) cudaFree(status);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "ct_vfactor_create"); ct_vfactor_free(F); return r; }
+    if (hs) {
+        ct_vfactor_free(F);
+        return fail(CT_ERR_ARG, "ct_vfactor_create: K(Z,Z) + jitter is not positive definite");
+    }
+    *out = F;
+    return CT_OK;
+}
+
+int ct_vfactor_embed(ct_vfactor* F, const double* x, int64_t n, float* v_out, float* p_out, void* stream) {
+    if (!F) return fail(CT_ERR_ARG, "ct_vfactor_embed: factor is NULL");
+    if (n < 0) return fail(CT_ERR_ARG, "ct_vfactor_embed: n < 0");
+    if (n == 0) return CT_OK;
+    if (!x || !v_out || !p_out) return fail(CT_ERR_ARG, "ct_vfactor_embed: NULL pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long want = ct::vmatrix_chunk_rows(n, F->m);
+    if (want > F->chunk) {
+        // grow the scratch; cudaFree waits for earlier embeds that still use it
+        if (F->kc) cudaFree(F->kc);
+        if (F->vc) cudaFree(F->vc);
+        F->kc = F->vc = nullptr;
+        F->chunk = 0;
+        CT_CUDA(cudaMalloc((void**)&F->kc, sizeof(double) * (size_t)want * F->m), "ct_vfactor_embed: scratch");
+        CT_CUDA(cudaMalloc((void**)&F->vc, sizeof(double) * (size_t)want * F->m), "ct_vfactor_embed: scratch");
+        F->chunk = want;
+    }
+    CT_CUDA(ct::vmatrix_embed(x, n, F->d, F->z, F->m, F->kernel_type, F->variance, F->lengthscale, F->Li, F->kc,
+                              F->vc, F->chunk, v_out, p_out, st, nullptr),
+            "ct_vfactor_embed launch");
+    return CT_OK;
+}
+
+int ct_vfactor_chol(const ct_vfactor* F, double* l_out, void* stream) {
+    if (!F || !l_out) return fail(CT_ERR_ARG, "ct_vfactor_chol: NULL argument");
+    CT_CUDA(cudaMemcpyAsync(l_out, F->L, sizeof(double) * (size_t)F->m * F->m, cudaMemcpyDeviceToDevice,
+                            (cudaStream_t)stream),
+            "ct_vfactor_chol copy");
+    return CT_OK;
+}
+
+int ct_vfactor_free(ct_vfactor* F) {
+    if (!F) return CT_OK;
+    if (F->z) cudaFree(F->z);
+    if (F->L) cudaFree(F->L);
+    if (F->Li) cudaFree(F->Li);
+    if (F->kc) cudaFree(F->kc);
+    if (F->vc) cudaFree(F->vc);
+    delete F;
     return CT_OK;
 }
 

@@ -152,6 +152,82 @@ class CudaResidualIndex:
             pass
 
 
+class CudaVFactor:
+    """FP64 factor of the residual backend on one GPU (``ct_vfactor_*``).
+
+    ``chol(K(Z,Z) + 1e-6 var I)`` and its inverse stay resident; :meth:`embed` turns
+    points (dataset rows, or new query points when serving) into f32 V rows and p
+    values exactly as build_residual_backend does for the dataset
+    (covertreex/metrics/residual/host_backend.py:202-219).
+    """
+
+    def __init__(self, inducing_points, *, kernel_type: int = 0, variance: float = 1.0, lengthscale: float = 1.0,
+                 device=None, stream=None):
+        torch = _torch()
+        self.device = torch.device(device if device is not None else "cuda")
+        L = _lib.load()
+        z = _as_device(inducing_points, torch.float64, self.device)
+        if z.dim() == 1:
+            z = z.reshape(-1, 1)
+        self.m, self.d = int(z.shape[0]), int(z.shape[1])
+        self.kernel_type, self.variance, self.lengthscale = int(kernel_type), float(variance), float(lengthscale)
+        self._h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(L.ct_vfactor_create(ctypes.c_void_p(z.data_ptr()), self.m, self.d, self.kernel_type,
+                                           self.variance, self.lengthscale, _stream_ptr(stream),
+                                           ctypes.byref(self._h)))
+
+    def embed_device(self, x, *, stream=None):
+        """V rows [n, m] and p [n] (device f32 tensors) for points x [n, d]."""
+        torch = _torch()
+        xs = _as_device(x, torch.float64, self.device)
+        if xs.dim() == 1:
+            xs = xs.reshape(-1, self.d)
+        if xs.shape[1] != self.d:
+            raise ValueError(f"points have {xs.shape[1]} coordinates, the factor {self.d}")
+        n = int(xs.shape[0])
+        v = torch.empty((n, self.m), dtype=torch.float32, device=self.device)
+        p = torch.empty((n,), dtype=torch.float32, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().ct_vfactor_embed(self._h, ctypes.c_void_p(xs.data_ptr()), n,
+                                                    ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(p.data_ptr()),
+                                                    _stream_ptr(stream)))
+        return v, p
+
+    def embed(self, x):
+        v, p = self.embed_device(x)
+        return v.cpu().numpy(), p.cpu().numpy()
+
+    def chol(self) -> np.ndarray:
+        torch = _torch()
+        out = torch.empty((self.m, self.m), dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().ct_vfactor_chol(self._h, ctypes.c_void_p(out.data_ptr()), _stream_ptr(None)))
+        return out.cpu().numpy()
+
+    def free(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().ct_vfactor_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
 def build_vmatrix_cuda(points: np.ndarray, inducing_idx: np.ndarray, *, kernel_type: int, variance: float,
                        lengthscale: float):
-    raise NotImplementedError("GPU V-matrix construction is not available in this build")
+    """V [N, m] f32, p [N] f32 and L [m, m] FP64 of build_residual_backend, on the GPU."""
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    if pts.ndim == 1:
+        pts = pts.reshape(-1, 1)
+    f = CudaVFactor(pts[np.asarray(inducing_idx, dtype=np.int64)], kernel_type=kernel_type, variance=variance,
+                    lengthscale=lengthscale)
+    try:
+        V, p = f.embed(pts)
+        L = f.chol()
+    finally:
+        f.free()
+    return V, p, L

@@ -52,7 +52,9 @@ class BuiltCoverTree:
 def cover_tree(coords: np.ndarray, *, kernel: Optional[Kernel] = None, v_matrix: Optional[np.ndarray] = None,
                p_diag: Optional[np.ndarray] = None, kernel_diag: Optional[np.ndarray] = None,
                inducing_count: int = 512, seed: int = 42, chunk_size: int = 512, engine: str = "cuda",
-               device: Any = None) -> BuiltCoverTree:
+               device: Any = None, vmatrix_device: str = "host") -> BuiltCoverTree:
+    """``vmatrix_device="cuda"`` builds V and p from ``kernel`` on the GPU in FP64
+    (``ct_vfactor_*``); the default ``"host"`` keeps the reference's numpy algebra."""
     coords_f32 = np.asarray(coords, dtype=np.float32)
     if coords_f32.ndim == 1:
         coords_f32 = coords_f32.reshape(-1, 1)
@@ -76,7 +78,8 @@ def cover_tree(coords: np.ndarray, *, kernel: Optional[Kernel] = None, v_matrix:
     else:
         backend = build_residual_backend(coords_f32, seed=seed, inducing_count=inducing_count,
                                          variance=kernel.variance, lengthscale=kernel.lengthscale,
-                                         chunk_size=chunk_size, kernel_type=kernel.kernel_type)
+                                         chunk_size=chunk_size, kernel_type=kernel.kernel_type,
+                                         device=vmatrix_device)
         params = {"variance": kernel.variance, "lengthscale": kernel.lengthscale,
                   "kernel_type": kernel.kernel_type, "chunk_size": chunk_size}
     engine_impl = get_engine(engine)

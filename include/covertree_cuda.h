@@ -162,6 +162,29 @@ CT_API int ct_debug_screen_dots(ct_tree* tree, const int32_t* rows_a, const int3
 /* n, m, d of a tree (host outputs; any may be NULL). */
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
 
+/*
+ * Residual-backend factor, built on the GPU in FP64.  Replaces the dense algebra of
+ * build_residual_backend (covertreex/metrics/residual/host_backend.py:202-219):
+ *   ct_vfactor_create  <- k_mm = K(Z, Z) + 1e-6 variance I; l_mm = cholesky(k_mm)
+ *                         (host_backend.py:207-212); also keeps l_mm^-1 on the device
+ *   ct_vfactor_embed   <- v = solve(l_mm, K(X, Z)^T)^T, p = max(variance - |v|^2, 1e-9),
+ *                         cast to f32 (host_backend.py:214-219 and 236-239); the same
+ *                         call embeds new query points for serving
+ *   ct_vfactor_chol    <- l_mm itself (m x m FP64, lower, zero upper triangle)
+ * z [m x d] and x [n x d] are device FP64 (the reference's float64 points and
+ * points[inducing_idx]); v_out [n x m] and p_out [n] device f32.  lengthscale is the
+ * scalar the reference's builder takes; kernel_type CT_KERNEL_*.  ct_vfactor_create
+ * synchronises `stream` and returns CT_ERR_ARG when k_mm is not positive definite
+ * (numpy's LinAlgError).  Embeds on one factor share its scratch: calls whose GPU work
+ * could overlap must use the same stream.
+ */
+typedef struct ct_vfactor ct_vfactor;
+CT_API int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type, double variance,
+                             double lengthscale, void* stream, ct_vfactor** out);
+CT_API int ct_vfactor_embed(ct_vfactor* f, const double* x, int64_t n, float* v_out, float* p_out, void* stream);
+CT_API int ct_vfactor_chol(const ct_vfactor* f, double* l_out, void* stream);
+CT_API int ct_vfactor_free(ct_vfactor* f);
+
 /* Release a tree and its device memory. */
 CT_API int ct_free(ct_tree* tree);
 

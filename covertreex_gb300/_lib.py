@@ -49,6 +49,16 @@ EXPORTED_SYMBOLS = (
     "ct_vfactor_embed",
     "ct_vfactor_chol",
     "ct_vfactor_free",
+    "ct_knn_residual_points",
+    "ct_batch_create",
+    "ct_batch_clear",
+    "ct_batch_add_ids",
+    "ct_batch_add_points",
+    "ct_batch_set_shape",
+    "ct_batch_autotune",
+    "ct_batch_run",
+    "ct_batch_get_shape",
+    "ct_batch_free",
 )
 
 
@@ -131,6 +141,27 @@ def load(build_if_missing: bool = True):
         L.ct_vfactor_chol.argtypes = [vp, vp, vp]
         L.ct_vfactor_free.restype = ctypes.c_int
         L.ct_vfactor_free.argtypes = [vp]
+        ip32 = ctypes.POINTER(i32)
+        L.ct_knn_residual_points.restype = ctypes.c_int
+        L.ct_knn_residual_points.argtypes = [vp, vp, vp, vp, i64, i32, vp, vp, ctypes.POINTER(CtStats), vp]
+        L.ct_batch_create.restype = ctypes.c_int
+        L.ct_batch_create.argtypes = [ctypes.POINTER(vp)]
+        L.ct_batch_clear.restype = ctypes.c_int
+        L.ct_batch_clear.argtypes = [vp]
+        L.ct_batch_add_ids.restype = ctypes.c_int
+        L.ct_batch_add_ids.argtypes = [vp, vp, vp, i64, i32, i32, vp, vp]
+        L.ct_batch_add_points.restype = ctypes.c_int
+        L.ct_batch_add_points.argtypes = [vp, vp, vp, vp, vp, i64, i32, vp, vp]
+        L.ct_batch_set_shape.restype = ctypes.c_int
+        L.ct_batch_set_shape.argtypes = [vp, i32, i32, i32]
+        L.ct_batch_autotune.restype = ctypes.c_int
+        L.ct_batch_autotune.argtypes = [vp, i32, vp, ip32, ip32, ip32]
+        L.ct_batch_run.restype = ctypes.c_int
+        L.ct_batch_run.argtypes = [vp, i32, ctypes.POINTER(CtStats), vp]
+        L.ct_batch_get_shape.restype = ctypes.c_int
+        L.ct_batch_get_shape.argtypes = [vp, ip32, ip32, ip32, ip32, ctypes.POINTER(i64)]
+        L.ct_batch_free.restype = ctypes.c_int
+        L.ct_batch_free.argtypes = [vp]
         _handle = L
         return L
 

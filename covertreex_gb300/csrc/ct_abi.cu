@@ -42,6 +42,7 @@ int cuda_fail(cudaError_t e, const char* where) {
 
 namespace ct {
 bool timing_enabled() { return g_timing; }
+int batch_fail(const char* where, const char* msg, int code) { return fail(code, "%s: %s", where, msg); }
 }  // namespace ct
 
 #define CT_CUDA(call, where)                          \
@@ -224,6 +225,27 @@ int ct_free(ct_tree* T) {
     if (!T) return CT_OK;
     delete T;
     return CT_OK;
+}
+
+int ct_knn_residual_points(ct_tree* T, const float* qv, const float* qp, const float* qcoords, int64_t nq, int32_t k,
+                           int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream) {
+    // one cached batch object per calling thread and device
+    thread_local ct_batch* tb = nullptr;
+    thread_local int tb_dev = -1;
+    if (!T) return fail(CT_ERR_ARG, "ct_knn_residual_points: tree is NULL");
+    int dev = 0;
+    CT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    if (tb && tb_dev != dev) { ct_batch_free(tb); tb = nullptr; }
+    if (!tb) {
+        int rc = ct_batch_create(&tb);
+        if (rc != CT_OK) return rc;
+        tb_dev = dev;
+    }
+    ct_batch_clear(tb);
+    int rc = ct_batch_add_points(tb, T, qv, qp, qcoords, nq, k, out_idx, out_dist);
+    if (rc == CT_OK) rc = ct_batch_run(tb, 0, stats, stream);
+    ct_batch_clear(tb);
+    return rc;
 }
 
 int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type, double variance,

@@ -1,317 +1,49 @@
-// ct_brute.cu — plain FP32 residual-correlation kNN, dense form.
+// ct_brute.cu — plain FP32 residual-correlation kNN, dense form for one tree.
 //
 // One CTA owns a tile of QT queries and sweeps every candidate (or, in
 // predecessor mode, every candidate with a smaller dataset index than the
-// tile's largest query).  Each thread holds a (QT/16) x 4 block of
-// query x candidate pairs.  The V dot product of a pair is evaluated in the
-// exact order of the reference's `dot_f32_simd_inline` (src/metric.rs:601-643):
-// sixteen lane accumulators, lane l summing elements 16c+l in c order with a
-// separately rounded multiply and add, then comb[l] = acc0[l] + acc1[l] and the
-// horizontal tree ((c0+c4)+(c2+c6)) + ((c1+c5)+(c3+c7)).  V is stored
-// residue-major (column l*(m/16)+c holds element 16c+l) so every lane
-// accumulator is a contiguous dot product over m/16 elements.  The epilogue is
-// the batch-path distance of src/metric.rs:439-485.  Top-k lists are kept in
-// shared memory in (dist, idx) order; a tile's candidates that beat the k-th
-// entry are merged by rank.
+// tile's largest query).  The tile itself (dot-product order, distance
+// epilogue, top-k merge) is dense::run_tile in ct_dense.cuh, shared with the
+// batched persistent kernel.
 #include "ct_common.cuh"
+#include "ct_dense.cuh"
 #include "ct_internal.h"
 
 namespace ct {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kCT = 64;  // candidates per tile
-
-// residue visiting order: (acc0[l], acc1[l]) pairs in reduction-tree order
-__constant__ int kResidueOrder[16] = {0, 8, 4, 12, 2, 10, 6, 14, 1, 9, 5, 13, 3, 11, 7, 15};
-
-struct BruteSmem {
-    // byte offsets
-    size_t a, b, ds, ld, li, tmp, xq, xc, nq, nc, pq, pc, qid, cnt, total;
-};
-
-__host__ __device__ inline BruteSmem brute_layout(int qt, int m, int d, int k) {
-    BruteSmem L;
-    const int m16 = m / 16;
-    size_t off = 0;
-    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 15) & ~size_t(15); return o; };
-    L.a = take(sizeof(float) * qt * (m + 1));
-    L.b = take(sizeof(float) * 2 * kCT * (m16 + 1));
-    L.ds = take(sizeof(float) * qt * (kCT + 1));
-    L.ld = take(sizeof(float) * qt * k);
-    L.li = take(sizeof(int) * qt * k);
-    L.tmp = take(sizeof(float) * 8 * 2 * 64 + sizeof(int) * 8 * 2 * 64);
-    L.xq = take(sizeof(float) * qt * d);
-    L.xc = take(sizeof(float) * kCT * d);
-    L.nq = take(sizeof(float) * qt);
-    L.nc = take(sizeof(float) * kCT);
-    L.pq = take(sizeof(float) * qt);
-    L.pc = take(sizeof(float) * kCT);
-    L.qid = take(sizeof(long long) * qt);
-    L.cnt = take(sizeof(int) * qt);
-    L.total = off;
-    return L;
-}
-
-__device__ __forceinline__ void cp_async4(void* smem_dst, const void* gsrc) {
-    unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc));
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
-
-// Merge the passing candidates of one tile into query qi's sorted list.
-// Called by one full warp.  cand_d/cand_i: lane's two slots (cj = lane, lane+32).
-__device__ void merge_tile_into_list(float* ld, int* li, int& cnt, int k, float d0, int i0, bool p0, float d1,
-                                     int i1, bool p1, float* td, int* ti, float* sd, int* si) {
-    const int lane = threadIdx.x & 31;
-    unsigned m0 = __ballot_sync(0xffffffffu, p0);
-    unsigned m1 = __ballot_sync(0xffffffffu, p1);
-    int n0 = __popc(m0);
-    int nnew = n0 + __popc(m1);
-    unsigned below = (1u << lane) - 1u;
-    if (p0) { int pos = __popc(m0 & below); td[pos] = d0; ti[pos] = i0; }
-    if (p1) { int pos = n0 + __popc(m1 & below); td[pos] = d1; ti[pos] = i1; }
-    __syncwarp();
-    // rank new entries among themselves -> sorted copy in sd/si
-    for (int e = lane; e < nnew; e += 32) {
-        float de = td[e]; int ie = ti[e];
-        int r = 0;
-        for (int f = 0; f < nnew; ++f) r += nb_less(td[f], ti[f], de, ie) ? 1 : 0;
-        sd[r] = de; si[r] = ie;
-    }
-    __syncwarp();
-    const int L = cnt;
-    // gather final positions in registers first, then write
-    float outd[4]; int outi[4]; int outp[4]; int no = 0;
-    float outd2[4]; int outi2[4]; int outp2[4]; int no2 = 0;
-    for (int e = lane; e < nnew; e += 32) {
-        float de = sd[e]; int ie = si[e];
-        int lo = 0, hi = L;  // #list entries < new
-        while (lo < hi) { int mid = (lo + hi) >> 1; if (nb_less(ld[mid], li[mid], de, ie)) lo = mid + 1; else hi = mid; }
-        outd[no] = de; outi[no] = ie; outp[no] = e + lo; ++no;
-    }
-    for (int e = lane; e < L; e += 32) {
-        float de = ld[e]; int ie = li[e];
-        int lo = 0, hi = nnew;  // #new entries < list entry
-        while (lo < hi) { int mid = (lo + hi) >> 1; if (nb_less(sd[mid], si[mid], de, ie)) lo = mid + 1; else hi = mid; }
-        outd2[no2] = de; outi2[no2] = ie; outp2[no2] = e + lo; ++no2;
-    }
-    __syncwarp();
-    for (int t = 0; t < no; ++t) if (outp[t] < k) { ld[outp[t]] = outd[t]; li[outp[t]] = outi[t]; }
-    for (int t = 0; t < no2; ++t) if (outp2[t] < k) { ld[outp2[t]] = outd2[t]; li[outp2[t]] = outi2[t]; }
-    __syncwarp();
-    cnt = min(k, L + nnew);
-}
+using dense::kThreads;
 
 template <int QT>
 __global__ void __launch_bounds__(kThreads, 1) brute_knn_kernel(BruteParams P) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const BruteSmem S = brute_layout(QT, P.m, P.d, P.k);
-    float* As = (float*)(smem_raw + S.a);
-    float* Bs = (float*)(smem_raw + S.b);
-    float* Ds = (float*)(smem_raw + S.ds);
-    float* Ld = (float*)(smem_raw + S.ld);
-    int* Li = (int*)(smem_raw + S.li);
-    float* Td = (float*)(smem_raw + S.tmp);
-    int* Ti = (int*)(Td + 8 * 2 * 64);
-    float* Xq = (float*)(smem_raw + S.xq);
-    float* Xc = (float*)(smem_raw + S.xc);
-    float* Nq = (float*)(smem_raw + S.nq);
-    float* Nc = (float*)(smem_raw + S.nc);
-    float* Pq = (float*)(smem_raw + S.pq);
-    float* Pc = (float*)(smem_raw + S.pc);
-    long long* Qid = (long long*)(smem_raw + S.qid);
-    int* Cnt = (int*)(smem_raw + S.cnt);
-
-    constexpr int QPT = QT / 16;  // queries per thread
-    const int tid = threadIdx.x;
-    const int lane = tid & 31, warp = tid >> 5;
-    const int tq = tid >> 4, tc = tid & 15;
-    const int m = P.m, m16 = m / 16, d = P.d, k = P.k;
-    const int AST = m + 1, BST = m16 + 1;
-    const long long n = P.n;
+    dense::Tile J;
+    J.vperm = P.vperm; J.xs = P.xs; J.norms = P.norms; J.p = P.p;
+    J.n = P.n; J.m = P.m; J.d = P.d; J.k = P.k; J.kernel_type = P.kernel_type; J.predecessor = P.predecessor;
+    J.var = P.var;
+    J.qids = P.qids; J.qv = nullptr; J.qcoords = nullptr; J.qp = nullptr; J.inv_ls = nullptr;
+    J.nq = P.nq;
     // heavy tiles (large query ids in predecessor mode) first
-    const long long tile = (long long)gridDim.x - 1 - blockIdx.x;
-    const long long q0 = tile * QT;
-
-    // ---- load query tile
-    for (int qi = tid; qi < QT; qi += kThreads) {
-        long long g = q0 + qi;
-        long long id = g < P.nq ? P.qids[g] : -1;
-        if (id >= P.n) id = -1;  // ids outside [0, n) give an all-padding row
-        if (id < 0) id = -1;
-        Qid[qi] = id;
-        Cnt[qi] = 0;
-        Nq[qi] = id >= 0 ? P.norms[id] : 0.f;
-        Pq[qi] = id >= 0 ? P.p[id] : 1.f;
-    }
-    __syncthreads();
-    for (int e = tid; e < QT * m; e += kThreads) {
-        int qi = e / m, c = e - qi * m;
-        long long id = Qid[qi];
-        As[qi * AST + c] = id >= 0 ? P.vperm[id * m + c] : 0.f;
-    }
-    for (int e = tid; e < QT * d; e += kThreads) {
-        int qi = e / d, c = e - qi * d;
-        long long id = Qid[qi];
-        Xq[e] = id >= 0 ? P.xs[id * d + c] : 0.f;
-    }
-    long long jend = n;
-    if (P.predecessor) {
-        long long mx = 0;
-        for (int qi = 0; qi < QT; ++qi) mx = Qid[qi] > mx ? Qid[qi] : mx;
-        jend = mx < n ? mx : n;
-    }
-    __syncthreads();
-
-    for (long long j0 = 0; j0 < jend; j0 += kCT) {
-        // candidate scalars
-        for (int cj = tid; cj < kCT; cj += kThreads) {
-            long long g = j0 + cj;
-            Nc[cj] = g < n ? P.norms[g] : 0.f;
-            Pc[cj] = g < n ? P.p[g] : 1.f;
-        }
-        for (int e = tid; e < kCT * d; e += kThreads) {
-            int cj = e / d, c = e - cj * d;
-            long long g = j0 + cj;
-            Xc[e] = g < n ? P.xs[g * d + c] : 0.f;
-        }
-        // prefetch residue 0
-        auto stage = [&](int s, int buf) {
-            const int l = kResidueOrder[s];
-            float* dst = Bs + buf * kCT * BST;
-            for (int e = tid; e < kCT * m16; e += kThreads) {
-                int cj = e / m16, c = e - cj * m16;
-                long long g = j0 + cj;
-                if (g < n) cp_async4(dst + cj * BST + c, P.vperm + g * m + l * m16 + c);
-                else dst[cj * BST + c] = 0.f;
-            }
-            cp_async_commit();
-        };
-        stage(0, 0);
-
-        float h[QPT][4], cA[QPT][4], sA[QPT][4], t0[QPT][4];
-        for (int s = 0; s < 16; ++s) {
-            cp_async_wait_all();
-            __syncthreads();
-            if (s + 1 < 16) stage(s + 1, (s + 1) & 1);
-            const int l = kResidueOrder[s];
-            const float* Bb = Bs + (s & 1) * kCT * BST;
-            float acc[QPT][4];
-#pragma unroll
-            for (int a = 0; a < QPT; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-            const float* Ab = As + l * m16;
-#pragma unroll 4
-            for (int c = 0; c < m16; ++c) {
-                float av[QPT], bv[4];
-#pragma unroll
-                for (int a = 0; a < QPT; ++a) av[a] = Ab[(tq + 16 * a) * AST + c];
-#pragma unroll
-                for (int b = 0; b < 4; ++b) bv[b] = Bb[(tc + 16 * b) * BST + c];
-#pragma unroll
-                for (int a = 0; a < QPT; ++a)
-#pragma unroll
-                    for (int b = 0; b < 4; ++b) acc[a][b] = __fadd_rn(__fmul_rn(av[a], bv[b]), acc[a][b]);
-            }
-            // fold into the reduction tree
-#pragma unroll
-            for (int a = 0; a < QPT; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    float v = acc[a][b];
-                    switch (s) {
-                        case 0: case 2: case 4: case 6: case 8: case 10: case 12: case 14:
-                            h[a][b] = v; break;
-                        case 1: case 5: case 9: case 13:
-                            cA[a][b] = __fadd_rn(h[a][b], v); break;
-                        case 3: case 11:
-                            sA[a][b] = __fadd_rn(cA[a][b], __fadd_rn(h[a][b], v)); break;
-                        case 7:
-                            t0[a][b] = __fadd_rn(sA[a][b], __fadd_rn(cA[a][b], __fadd_rn(h[a][b], v))); break;
-                        case 15: {
-                            float s3 = __fadd_rn(cA[a][b], __fadd_rn(h[a][b], v));
-                            float t1 = __fadd_rn(sA[a][b], s3);
-                            h[a][b] = __fadd_rn(t0[a][b], t1);  // final dot in h
-                        } break;
-                    }
-                }
-        }
-        // ---- epilogue: distances into Ds
-#pragma unroll
-        for (int a = 0; a < QPT; ++a) {
-            const int qi = tq + 16 * a;
-            const long long gq = Qid[qi];
-#pragma unroll
-            for (int b = 0; b < 4; ++b) {
-                const int cj = tc + 16 * b;
-                const long long gc = j0 + cj;
-                float dist = __int_as_float(0x7f800000);
-                bool valid = gq >= 0 && gc < n && (!P.predecessor || gc < gq);
-                if (valid) {
-                    if (gq == gc) {
-                        dist = 0.f;
-                    } else {
-                        float d2 = coord_d2_batch(Xq + qi * d, Xc + cj * d, d, Nq[qi], Nc[cj]);
-                        float kv = kernel_value_batch(d2, P.var, P.kernel_type);
-                        dist = residual_from_parts(kv, h[a][b], Pq[qi], Pc[cj]);
-                    }
-                }
-                Ds[qi * (kCT + 1) + cj] = dist;
-            }
-        }
-        __syncthreads();
-        // ---- selection: warp w owns queries w, w+8, ...
-        float* td = Td + warp * 2 * 64;
-        int* ti = Ti + warp * 2 * 64;
-        for (int qi = warp; qi < QT; qi += kThreads / 32) {
-            if (Qid[qi] < 0) continue;
-            int cnt = Cnt[qi];
-            float* ld = Ld + qi * k;
-            int* li = Li + qi * k;
-            float taud = cnt >= k ? ld[k - 1] : __int_as_float(0x7f800000);
-            int taui = cnt >= k ? li[k - 1] : 0x7fffffff;
-            float d0 = Ds[qi * (kCT + 1) + lane];
-            float d1 = Ds[qi * (kCT + 1) + lane + 32];
-            int i0 = (int)(j0 + lane), i1 = (int)(j0 + lane + 32);
-            bool p0 = d0 < __int_as_float(0x7f800000) && (cnt < k || nb_less(d0, i0, taud, taui));
-            bool p1 = d1 < __int_as_float(0x7f800000) && (cnt < k || nb_less(d1, i1, taud, taui));
-            if (__any_sync(0xffffffffu, p0 || p1)) {
-                merge_tile_into_list(ld, li, cnt, k, d0, i0, p0, d1, i1, p1, td, ti, td + 64, ti + 64);
-                if (lane == 0) Cnt[qi] = cnt;
-            }
-        }
-        __syncthreads();
-    }
-
-    // ---- write results (dataset ids; -1 / FLT_MAX padding)
-    for (int e = tid; e < QT * k; e += kThreads) {
-        int qi = e / k, j = e - qi * k;
-        long long g = q0 + qi;
-        if (g >= P.nq) continue;
-        int cnt = Cnt[qi];
-        bool ok = j < cnt;
-        P.out_idx[g * k + j] = ok ? (long long)Li[qi * k + j] : -1LL;
-        P.out_dist[g * k + j] = ok ? Ld[qi * k + j] : CT_FLT_MAX;
-    }
+    J.q0 = ((long long)gridDim.x - 1 - blockIdx.x) * QT;
+    J.cbeg = 0; J.cend = P.n;
+    J.out_idx = P.out_idx; J.out_dist = P.out_dist; J.out_stride = P.k;
+    dense::run_tile<QT>(J, smem_raw);
 }
 
 }  // namespace
 
-size_t brute_smem_bytes(int qt, int m, int d, int k) { return brute_layout(qt, m, d, k).total; }
+size_t brute_smem_bytes(int qt, int m, int d, int k) { return dense::layout(qt, m, d, k).total; }
 
 int brute_pick_qt(int m, int d, int k, size_t smem_limit) {
     const int qts[3] = {64, 32, 16};
     for (int t = 0; t < 3; ++t)
-        if (brute_layout(qts[t], m, d, k).total <= smem_limit) return qts[t];
+        if (dense::layout(qts[t], m, d, k).total <= smem_limit) return qts[t];
     return 0;
 }
 
 cudaError_t launch_brute_knn(const BruteParams& P, int qt, cudaStream_t stream) {
-    const size_t smem = brute_layout(qt, P.m, P.d, P.k).total;
+    const size_t smem = dense::layout(qt, P.m, P.d, P.k).total;
     const long long tiles = (P.nq + qt - 1) / qt;
     if (tiles <= 0) return cudaSuccess;
     dim3 grid((unsigned)tiles), block(kThreads);

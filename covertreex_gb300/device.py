@@ -109,6 +109,28 @@ class CudaResidualIndex:
         idx, dist = self.knn_device(q, k, predecessor=predecessor, form=form)
         return idx.cpu().numpy(), dist.cpu().numpy()
 
+    def knn_points_device(self, qv, qp, qcoords, k: int, *, stream=None, out=None):
+        """kNN of NEW points: V rows qv [Q,m] (e.g. from CudaVFactor.embed_device), p values
+        qp [Q] and raw coordinates qcoords [Q,d].  Returns (idx, dist) CUDA tensors."""
+        torch = _torch()
+        qv = _as_device(qv, torch.float32, self.device)
+        qp = _as_device(qp, torch.float32, self.device).reshape(-1)
+        qc = _as_device(qcoords, torch.float32, self.device).reshape(qp.shape[0], self.d)
+        if qv.shape != (qp.shape[0], self.m):
+            raise ValueError(f"qv must be [Q, {self.m}]")
+        nq, k = int(qp.shape[0]), int(k)
+        if out is None:
+            idx = torch.empty((nq, k), dtype=torch.int64, device=self.device)
+            dist = torch.empty((nq, k), dtype=torch.float32, device=self.device)
+        else:
+            idx, dist = out
+        st = _lib.CtStats()
+        _lib.check(_lib.load().ct_knn_residual_points(self._h, qv.data_ptr(), qp.data_ptr(), qc.data_ptr(), nq, k,
+                                                      idx.data_ptr(), dist.data_ptr(), ctypes.byref(st),
+                                                      _stream_ptr(stream)))
+        self.last_stats = st.as_dict()
+        return idx, dist
+
     def debug_screen_dots(self, rows_a, rows_b):
         """Raw BF16-screened dot products (hi.hi + hi.lo + lo.hi) of 128 x 256 dataset rows."""
         torch = _torch()
@@ -144,6 +166,90 @@ class CudaResidualIndex:
         if getattr(self, "_h", None) is not None and self._h.value:
             _lib.load().ct_free(self._h)
         self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class CudaBatch:
+    """Batching form (``ct_batch_*``): query sets against many resident
+    :class:`CudaResidualIndex` trees in one persistent launch, optionally replayed
+    as a CUDA graph.  Outputs are allocated here and returned by ``add_*``; they are
+    valid once :meth:`run` has completed on its stream."""
+
+    def __init__(self, device=None):
+        torch = _torch()
+        self.device = torch.device(device if device is not None else "cuda")
+        self._h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().ct_batch_create(ctypes.byref(self._h)))
+        self._keep: list = []
+        self.last_stats: dict = {}
+
+    def _outputs(self, nq, k, out):
+        torch = _torch()
+        if out is not None:
+            return out
+        return (torch.empty((nq, k), dtype=torch.int64, device=self.device),
+                torch.empty((nq, k), dtype=torch.float32, device=self.device))
+
+    def add_ids(self, index: CudaResidualIndex, q_ids, k: int, *, predecessor: bool = False, out=None):
+        torch = _torch()
+        q = _as_device(q_ids, torch.int64, self.device).reshape(-1)
+        idx, dist = self._outputs(int(q.shape[0]), int(k), out)
+        _lib.check(_lib.load().ct_batch_add_ids(self._h, index._h, q.data_ptr(), int(q.shape[0]), int(k),
+                                                1 if predecessor else 0, idx.data_ptr(), dist.data_ptr()))
+        self._keep += [index, q, idx, dist]
+        return idx, dist
+
+    def add_points(self, index: CudaResidualIndex, qv, qp, qcoords, k: int, *, out=None):
+        torch = _torch()
+        qv = _as_device(qv, torch.float32, self.device)
+        qp = _as_device(qp, torch.float32, self.device).reshape(-1)
+        qc = _as_device(qcoords, torch.float32, self.device).reshape(qp.shape[0], index.d)
+        if qv.shape != (qp.shape[0], index.m):
+            raise ValueError(f"qv must be [Q, {index.m}]")
+        idx, dist = self._outputs(int(qp.shape[0]), int(k), out)
+        _lib.check(_lib.load().ct_batch_add_points(self._h, index._h, qv.data_ptr(), qp.data_ptr(), qc.data_ptr(),
+                                                   int(qp.shape[0]), int(k), idx.data_ptr(), dist.data_ptr()))
+        self._keep += [index, qv, qp, qc, idx, dist]
+        return idx, dist
+
+    def set_shape(self, qt: int = 0, ctas_per_sm: int = 0, items_per_slot: int = 0):
+        _lib.check(_lib.load().ct_batch_set_shape(self._h, int(qt), int(ctas_per_sm), int(items_per_slot)))
+
+    def autotune(self, reps: int = 1, stream=None):
+        q, c, i = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(_lib.load().ct_batch_autotune(self._h, int(reps), _stream_ptr(stream), ctypes.byref(q),
+                                                 ctypes.byref(c), ctypes.byref(i)))
+        return {"qt": q.value, "ctas_per_sm": c.value, "items_per_slot": i.value}
+
+    def run(self, *, use_graph: bool = True, stream=None):
+        st = _lib.CtStats()
+        _lib.check(_lib.load().ct_batch_run(self._h, 1 if use_graph else 0, ctypes.byref(st), _stream_ptr(stream)))
+        self.last_stats = st.as_dict()
+        return self.last_stats
+
+    def shape(self):
+        q, c, i, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        items = ctypes.c_int64()
+        _lib.check(_lib.load().ct_batch_get_shape(self._h, ctypes.byref(q), ctypes.byref(c), ctypes.byref(i),
+                                                  ctypes.byref(g), ctypes.byref(items)))
+        return {"qt": q.value, "ctas_per_sm": c.value, "items_per_slot": i.value, "grid": g.value,
+                "items": items.value}
+
+    def clear(self):
+        _lib.check(_lib.load().ct_batch_clear(self._h))
+        self._keep = []
+
+    def free(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().ct_batch_free(self._h)
+        self._h = None
+        self._keep = []
 
     def __del__(self):
         try:

@@ -163,6 +163,50 @@ CT_API int ct_debug_screen_dots(ct_tree* tree, const int32_t* rows_a, const int3
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
 
 /*
+ * k nearest dataset rows of NEW points (no counterpart in the reference, whose
+ * queries are dataset ids only).  Query row i is qv[i] [m] (natural column order,
+ * as ct_vfactor_embed writes it), qp[i] and qcoords[i] [d] (unscaled); all device f32.
+ * Each point is scaled, normalised and compared exactly like one more dataset row
+ * would be (plain FP32, the dense form's arithmetic).  k <= 128.
+ */
+CT_API int ct_knn_residual_points(ct_tree* tree, const float* qv, const float* qp, const float* qcoords, int64_t nq,
+                                  int32_t k, int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream);
+
+/*
+ * Batching form: many query sets against many resident trees in ONE persistent
+ * kernel launch that drains a device work queue of (query set, query tile,
+ * candidate chunk) items; with use_graph the launch (descriptor copy + kernel) is
+ * replayed from a CUDA graph.  No counterpart in the reference, which runs one
+ * tree's knn_query_residual per call (src/lib.rs:370-507).
+ *   ct_batch_add_ids     a query set of dataset ids (same contract as ct_knn_residual,
+ *                        CT_FORM_DENSE: bit-identical output)
+ *   ct_batch_add_points  a query set of new points (same contract as ct_knn_residual_points)
+ *   ct_batch_set_shape   fix the launch shape: qt (queries per CTA tile: 16/32/64),
+ *                        ctas_per_sm (1/2), items_per_slot (candidate-split target); 0 = auto
+ *   ct_batch_autotune    time the candidate shapes on the current batch (reps runs each,
+ *                        synchronising `stream`) and keep the fastest
+ *   ct_batch_run         launch every added query set; asynchronous on `stream`
+ *   ct_batch_get_shape   shape, grid and work-item count of the last run
+ * Added query sets keep pointers to the caller's device buffers, which must stay
+ * valid until the run completes.  Results do not depend on the shape or on the
+ * other query sets of the batch.  One batch object serves one stream at a time.
+ */
+typedef struct ct_batch ct_batch;
+CT_API int ct_batch_create(ct_batch** out);
+CT_API int ct_batch_clear(ct_batch* b);
+CT_API int ct_batch_add_ids(ct_batch* b, ct_tree* tree, const int64_t* q_ids, int64_t nq, int32_t k,
+                            int32_t predecessor, int64_t* out_idx, float* out_dist);
+CT_API int ct_batch_add_points(ct_batch* b, ct_tree* tree, const float* qv, const float* qp, const float* qcoords,
+                               int64_t nq, int32_t k, int64_t* out_idx, float* out_dist);
+CT_API int ct_batch_set_shape(ct_batch* b, int32_t qt, int32_t ctas_per_sm, int32_t items_per_slot);
+CT_API int ct_batch_autotune(ct_batch* b, int32_t reps, void* stream, int32_t* qt, int32_t* ctas_per_sm,
+                             int32_t* items_per_slot);
+CT_API int ct_batch_run(ct_batch* b, int32_t use_graph, ct_stats* stats, void* stream);
+CT_API int ct_batch_get_shape(const ct_batch* b, int32_t* qt, int32_t* ctas_per_sm, int32_t* items_per_slot,
+                              int32_t* grid, int64_t* items);
+CT_API int ct_batch_free(ct_batch* b);
+
+/*
  * Residual-backend factor, built on the GPU in FP64.  Replaces the dense algebra of
  * build_residual_backend (covertreex/metrics/residual/host_backend.py:202-219):
  *   ct_vfactor_create  <- k_mm = K(Z, Z) + 1e-6 variance I; l_mm = cholesky(k_mm)

@@ -972,6 +972,54 @@ CT_EXPORT int64_t ct_oracle_knn_residual(const ct_otree* H, const int64_t* queri
 /* Brute force over the batch-path f32 distance: the exact answer the        */
 /* traversal approximates (ties by lower dataset index).  Dataset numbering. */
 /* ------------------------------------------------------------------------- */
+/* New points against a dataset: query row i is (qv[i], qp[i], qcoords[i]) and is
+ * scaled, normalised and compared exactly like one more dataset row would be
+ * (metric_init + dist_batch above); candidates are the n dataset rows.  The
+ * reference has no new-point query; this is the f32 oracle of the serving path. */
+CT_EXPORT void ct_oracle_brute_points_f32(const float* v, const float* p, const float* coords, int64_t n, int m,
+                                          int d, float var, const float* ls, int n_ls, int kernel_type,
+                                          const float* qv, const float* qp, const float* qcoords, int64_t nq,
+                                          int k, int64_t* out_idx, float* out_dist, int n_threads) {
+    const int64_t nt = n + nq;
+    float* av = (float*)malloc(sizeof(float) * (size_t)(nt > 0 ? nt : 1) * (size_t)m);
+    float* ap = (float*)malloc(sizeof(float) * (size_t)(nt > 0 ? nt : 1));
+    float* ac = (float*)malloc(sizeof(float) * (size_t)(nt > 0 ? nt : 1) * (size_t)d);
+    memcpy(av, v, sizeof(float) * (size_t)n * m);
+    memcpy(av + (size_t)n * m, qv, sizeof(float) * (size_t)nq * m);
+    memcpy(ap, p, sizeof(float) * (size_t)n);
+    memcpy(ap + n, qp, sizeof(float) * (size_t)nq);
+    memcpy(ac, coords, sizeof(float) * (size_t)n * d);
+    memcpy(ac + (size_t)n * d, qcoords, sizeof(float) * (size_t)nq * d);
+    ct_metric M;
+    metric_init(&M, av, ap, ac, nt, m, d, var, ls, n_ls, kernel_type, 0);
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    #pragma omp parallel
+    {
+        nb* buf = (nb*)malloc(sizeof(nb) * (size_t)(k + 2));
+        #pragma omp for schedule(dynamic, 16)
+        for (int64_t qi = 0; qi < nq; ++qi) {
+            nheap h = {buf, 0, k};
+            for (int64_t j = 0; j < n; ++j) {
+                nb x = {dist_batch(&M, n + qi, j), j};
+                if (h.n < k) nh_push(&h, x);
+                else if (nb_less(x, h.a[0])) { h.a[0] = x; int c = 0; for (;;) { int l = 2*c+1, r = l+1, g = c; if (l < h.n && nb_less(h.a[g], h.a[l])) g = l; if (r < h.n && nb_less(h.a[g], h.a[r])) g = r; if (g == c) break; nb t = h.a[g]; h.a[g] = h.a[c]; h.a[c] = t; c = g; } }
+            }
+            qsort(h.a, (size_t)h.n, sizeof(nb), cmp_nb);
+            for (int j = 0; j < k; ++j) {
+                out_idx[qi * k + j] = j < h.n ? h.a[j].i : -1;
+                out_dist[qi * k + j] = j < h.n ? h.a[j].d : FLT_MAX;
+            }
+        }
+        free(buf);
+    }
+    metric_free(&M);
+    free(av); free(ap); free(ac);
+}
+
 CT_EXPORT void ct_oracle_brute_f32(const float* v, const float* p, const float* coords, int64_t n, int m, int d,
                                    float var, const float* ls, int n_ls, int kernel_type,
                                    const int64_t* queries, int64_t nq, int k, int predecessor,
@@ -1080,7 +1128,8 @@ CT_EXPORT void ct_oracle_knn_euclidean(const ct_oetree* E, const float* queries,
                 { int c = 0; for (;;) { int l = 2*c+1, r = l+1, g = c;
                     if (l < nc && (ch[l].d < ch[g].d || (ch[l].d == ch[g].d && ch[l].i < ch[g].i))) g = l;
                     if (r < nc && (ch[r].d < ch[g].d || (ch[r].d == ch[g].d && ch[r].i < ch[g].i))) g = r;
-                    if (g == c) break; cand_t t = ch[g]; ch[g] = ch[c]; ch[c] = t; c = g; } }
+                    if (g == c) break;
+                    cand_t t = ch[g]; ch[g] = ch[c]; ch[c] = t; c = g; } }
                 int can_prune = res.n >= k;
                 if (can_prune) {
                     float radius = ldexpf(1.0f, T->levels[top.i] + 1);

@@ -75,6 +75,11 @@ def lib():
     L.ct_oracle_brute_f32.argtypes = [_f32p, _f32p, _f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_float, _f32p, ctypes.c_int, ctypes.c_int,
                                       _i64p, ctypes.c_int64, ctypes.c_int, ctypes.c_int, _i64p, _f32p, ctypes.c_int]
+    L.ct_oracle_brute_points_f32.restype = None
+    L.ct_oracle_brute_points_f32.argtypes = [_f32p, _f32p, _f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_float, _f32p, ctypes.c_int, ctypes.c_int,
+                                             _f32p, _f32p, _f32p, ctypes.c_int64, ctypes.c_int, _i64p, _f32p,
+                                             ctypes.c_int]
     L.ct_oracle_pair_dist.restype = None
     L.ct_oracle_pair_dist.argtypes = [_f32p, _f32p, _f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_float, _f32p, ctypes.c_int, ctypes.c_int,
@@ -269,6 +274,23 @@ def brute_knn_f32(V, p, coords, var, ls, kernel_type, queries, k, predecessor, t
     L.ct_oracle_brute_f32(_p(V, _f32p), _p(p, _f32p), _p(coords, _f32p), V.shape[0], V.shape[1], coords.shape[1],
                           float(var), _p(ls, _f32p), ls.size, int(kernel_type), _p(q, _i64p), q.size, int(k),
                           int(predecessor), _p(oi, _i64p), _p(od, _f32p), int(threads))
+    return oi, od
+
+
+def brute_knn_points_f32(V, p, coords, var, ls, kernel_type, qv, qp, qcoords, k, threads=0):
+    """Exact kNN of new points (rows qv/qp/qcoords) over the batch-path f32 distance,
+    each point handled like one more dataset row; candidates = the dataset."""
+    L = lib()
+    V = _c(V, np.float32); p = _c(p, np.float32); coords = _c(coords, np.float32)
+    qv = _c(qv, np.float32); qp = _c(qp, np.float32).reshape(-1); qcoords = _c(qcoords, np.float32)
+    ls = _c(np.atleast_1d(ls), np.float32)
+    nq = qp.size
+    oi = np.empty((nq, k), np.int64)
+    od = np.empty((nq, k), np.float32)
+    L.ct_oracle_brute_points_f32(_p(V, _f32p), _p(p, _f32p), _p(coords, _f32p), V.shape[0], V.shape[1],
+                                 coords.shape[1], float(var), _p(ls, _f32p), ls.size, int(kernel_type),
+                                 _p(qv, _f32p), _p(qp, _f32p), _p(qcoords, _f32p), nq, int(k), _p(oi, _i64p),
+                                 _p(od, _f32p), int(threads))
     return oi, od
 
 

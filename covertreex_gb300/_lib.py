@@ -143,7 +143,7 @@ def load(build_if_missing: bool = True):
         L.ct_vfactor_free.argtypes = [vp]
         ip32 = ctypes.POINTER(i32)
         L.ct_knn_residual_points.restype = ctypes.c_int
-        L.ct_knn_residual_points.argtypes = [vp, vp, vp, vp, i64, i32, vp, vp, ctypes.POINTER(CtStats), vp]
+        L.ct_knn_residual_points.argtypes = [vp, vp, vp, vp, i64, i32, i32, vp, vp, ctypes.POINTER(CtStats), vp]
         L.ct_batch_create.restype = ctypes.c_int
         L.ct_batch_create.argtypes = [ctypes.POINTER(vp)]
         L.ct_batch_clear.restype = ctypes.c_int

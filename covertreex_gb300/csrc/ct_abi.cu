@@ -228,11 +228,23 @@ int ct_free(ct_tree* T) {
 }
 
 int ct_knn_residual_points(ct_tree* T, const float* qv, const float* qp, const float* qcoords, int64_t nq, int32_t k,
-                           int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream) {
+                           int32_t form, int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream) {
     // one cached batch object per calling thread and device
     thread_local ct_batch* tb = nullptr;
     thread_local int tb_dev = -1;
     if (!T) return fail(CT_ERR_ARG, "ct_knn_residual_points: tree is NULL");
+    if (nq < 0) return fail(CT_ERR_ARG, "ct_knn_residual_points: nq < 0");
+    if (k <= 0) return fail(CT_ERR_ARG, "ct_knn_residual_points: k=%d must be positive", k);
+    if (k > 128) return fail(CT_ERR_UNSUPPORTED, "ct_knn_residual_points: k=%d above the supported maximum 128", k);
+    if (nq > 0 && (!qv || !qp || !qcoords || !out_idx || !out_dist))
+        return fail(CT_ERR_ARG, "ct_knn_residual_points: NULL pointer");
+    if (form == CT_FORM_SCREENED) {
+        if (stats) memset(stats, 0, sizeof(*stats));
+        return T->knn_screened_points(qv, qp, qcoords, nq, k, out_idx, out_dist, stats, (cudaStream_t)stream)
+                   ? fail(CT_ERR_STATE, "ct_knn_residual_points: screened form: %s", T->err)
+                   : CT_OK;
+    }
+    if (form != CT_FORM_DENSE) return fail(CT_ERR_ARG, "ct_knn_residual_points: form %d (dense or screened)", form);
     int dev = 0;
     CT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
     if (tb && tb_dev != dev) { ct_batch_free(tb); tb = nullptr; }

@@ -33,7 +33,9 @@ cudaError_t launch_metric_setup(const float* v, const float* p, const float* coo
 
 // ct_order.cu
 cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st,
-                          unsigned long long* keys_by_id = nullptr);
+                          unsigned long long* keys_by_id = nullptr, double* bounds_out = nullptr);
+cudaError_t hilbert_keys_bounded(const float* coords, long long n, int d, const double* bounds,
+                                 unsigned long long* keys, int* scratch_vals, cudaStream_t st);
 cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long long* ktmp, int* vtmp, long long n,
                              int kbits, unsigned* hist, void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st,
                              bool* result_in_tmp);

@@ -249,7 +249,7 @@ int radix_num_blocks(long long n) { return (int)((n + kTile - 1) / kTile); }
 // Compute the batch order of `coords` (n x d, f32): order[i] = dataset row of
 // sorted position i.  mode 1 = Hilbert (D-generic), 2 = Morton (D == 3 only).
 cudaError_t compute_order(const float* coords, long long n, int d, int mode, int* order_out, cudaStream_t st,
-                          unsigned long long* keys_by_id) {
+                          unsigned long long* keys_by_id, double* bounds_out) {
     if (n <= 0) return cudaSuccess;
     double* mm = nullptr;
     unsigned long long *keys = nullptr, *ktmp = nullptr;
@@ -285,6 +285,8 @@ cudaError_t compute_order(const float* coords, long long n, int d, int mode, int
         e = cudaGetLastError();
         if (e == cudaSuccess && keys_by_id)
             e = cudaMemcpyAsync(keys_by_id, keys, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess && bounds_out)
+            e = cudaMemcpyAsync(bounds_out, mm, sizeof(double) * 2 * 64, cudaMemcpyDeviceToDevice, st);
         bool in_tmp = false;
         if (e == cudaSuccess) e = radix_sort_pairs(keys, order_out, ktmp, vtmp, n, kbits, hist, scan, scan_bytes, st, &in_tmp);
         if (e == cudaSuccess && in_tmp) e = cudaMemcpyAsync(order_out, vtmp, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
@@ -292,6 +294,15 @@ cudaError_t compute_order(const float* coords, long long n, int d, int mode, int
     cudaFreeAsync(mm, st); cudaFreeAsync(keys, st); cudaFreeAsync(ktmp, st); cudaFreeAsync(vtmp, st);
     cudaFreeAsync(hist, st); cudaFreeAsync(scan, st);
     return e;
+}
+
+// Hilbert keys of points in the frame of bounds computed by compute_order for
+// another point set (coordinates outside it clamp to the edge cells).
+cudaError_t hilbert_keys_bounded(const float* coords, long long n, int d, const double* bounds,
+                                 unsigned long long* keys, int* scratch_vals, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    hilbert_keys_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(coords, n, d, bounds, keys, scratch_vals);
+    return cudaGetLastError();
 }
 
 }  // namespace ct

@@ -30,6 +30,7 @@
 // accumulation inside the tensor core (one rounding per MMA step plus the
 // step's internal alignment), both relative to sum |v_qi v_ci| <= ||v_q|| ||v_c||.
 #include <cuda_bf16.h>
+#include <string.h>
 
 #include <algorithm>
 #include <cmath>
@@ -797,6 +798,10 @@ struct State {
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
     double* inv_ls64 = nullptr;
     int* status = nullptr;
+    double* bounds = nullptr;               // Hilbert quantisation frame of the dataset (min/max per axis)
+    // query slab: rows [n, n + slab_cap) of the query-side arrays hold new points
+    long long slab_cap = 0;
+    cudaEvent_t slab_done = nullptr;        // last call that read the slab
 };
 
 constexpr int kFirstPrefixLog2 = 10;  // prefixes below 1024 points: every predecessor is rescored
@@ -912,6 +917,8 @@ void ct_tree::release_screen() {
     cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
     cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
+    cudaFree(S->bounds);
+    if (S->slab_done) cudaEventDestroy(S->slab_done);
     delete S;
     screen = nullptr;
 }
@@ -952,8 +959,9 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->xmax, sizeof(float) * n);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->status, sizeof(int));
+    A((void**)&S->bounds, sizeof(double) * 2 * 64);
     if (e != cudaSuccess) return T->set_err(CT_ERR_NOMEM, "screen prep allocation: %s", cudaGetErrorString(e));
-    e = ct::compute_order(T->coords_raw, n, T->d, 1, S->hil_order, st, S->hil_key);
+    e = ct::compute_order(T->coords_raw, n, T->d, 1, S->hil_order, st, S->hil_key, S->bounds);
     std::vector<int> order_h(n);
     std::vector<unsigned long long> key_h(n);
     if (e == cudaSuccess) {
@@ -997,7 +1005,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
 }
 
 int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
-                          ct_stats* stats, cudaStream_t st) {
+                          ct_stats* stats, cudaStream_t st, long long id_limit) {
     if (d > kMaxD) return set_err(CT_ERR_UNSUPPORTED, "screened form supports d <= %d (got %d)", kMaxD, d);
     if (m % KC != 0 || m > 1024) return set_err(CT_ERR_UNSUPPORTED, "screened form needs m %% 32 == 0 and m <= 1024 (got %d)", m);
     if (k > kMaxK) return set_err(CT_ERR_UNSUPPORTED, "screened form supports k <= %d (got %d)", kMaxK, k);
@@ -1042,7 +1050,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     A((void**)&evals_d, sizeof(long long));
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
 
-    slot_ids_kernel<<<grid_for(nq), 256, 0, st>>>((const long long*)q_ids, nq, n, slot_id, key_lvl, val_lvl,
+    slot_ids_kernel<<<grid_for(nq), 256, 0, st>>>((const long long*)q_ids, nq, id_limit > 0 ? id_limit : n,
+                                                 slot_id, key_lvl, val_lvl,
                                                  S->hil_key, S->lvl_key, S->lvl_meta, nlev, predecessor ? 1 : 0);
     ++launches;
     bool in_tmp = false;
@@ -1254,6 +1263,97 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         stats->overflow_queries = nfull;
     }
     return CT_OK;
+}
+
+// ---------------------------------------------------------------- new points
+namespace {
+
+__global__ void scale_rows_kernel(const float* __restrict__ coords, long long n, int d,
+                                  const float* __restrict__ inv_ls, float* __restrict__ xs) {
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (e >= n * d) return;
+    xs[e] = __fmul_rn(coords[e], inv_ls[e % d]);
+}
+
+__global__ void iota64_kernel(long long* a, long long n, long long base) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) a[i] = base + i;
+}
+
+// Grow the query-side arrays (V, scaled and raw coordinates, p, and the screened
+// form's per-row scalars and Hilbert keys) to n + rows rows.  Rows < n are copied;
+// the device is synchronised first because in-flight work may read the old arrays.
+int ensure_slab(ct_tree* T, State* S, long long rows) {
+    if (rows <= S->slab_cap) return CT_OK;
+    long long cap = std::max<long long>(rows, std::min<long long>(2 * S->slab_cap, 1LL << 20));
+    cap = std::max<long long>(cap, 4096);
+    if (T->n + cap >= (1LL << 31)) return T->set_err(CT_ERR_UNSUPPORTED, "%s", "query slab beyond 2^31 rows");
+    cudaError_t e = cudaDeviceSynchronize();
+    const size_t n = (size_t)T->n, tot = (size_t)(T->n + cap);
+    auto grow = [&](void** ptr, size_t row_bytes) {
+        void* np = nullptr;
+        if (e == cudaSuccess) e = cudaMalloc(&np, row_bytes * tot);
+        if (e == cudaSuccess) e = cudaMemcpy(np, *ptr, row_bytes * n, cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess) { cudaFree(*ptr); *ptr = np; }
+        else if (np) cudaFree(np);
+    };
+    grow((void**)&T->vnat, sizeof(float) * T->m);
+    grow((void**)&T->xs, sizeof(float) * T->d);
+    grow((void**)&T->coords_raw, sizeof(float) * T->d);
+    grow((void**)&T->p, sizeof(float));
+    grow((void**)&S->vn, sizeof(float));
+    grow((void**)&S->isp, sizeof(float));
+    grow((void**)&S->xmax, sizeof(float));
+    grow((void**)&S->hil_key, sizeof(unsigned long long));
+    if (e == cudaSuccess && !S->slab_done) e = cudaEventCreateWithFlags(&S->slab_done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return T->set_err(CT_ERR_NOMEM, "query slab of %lld rows: %s", cap, cudaGetErrorString(e));
+    S->slab_cap = cap;
+    return CT_OK;
+}
+
+}  // namespace
+
+// kNN of new points with the screened form: the points are written to the query
+// slab (rows n .. n+nq-1, with the dataset's own scaling, scalars and Hilbert
+// frame) and searched as query ids n + i against the n dataset rows.  Calls on one
+// tree take turns on the slab through an event.
+int ct_tree::knn_screened_points(const float* qv, const float* qp, const float* qcoords, int64_t nq, int k,
+                                 int64_t* out_idx, float* out_dist, ct_stats* stats, cudaStream_t st) {
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nq <= 0) return CT_OK;
+    if (d > kMaxD) return set_err(CT_ERR_UNSUPPORTED, "screened form supports d <= %d (got %d)", kMaxD, d);
+    int rc = screen_prepare(this, st);
+    if (rc != CT_OK) return rc;
+    State* S = (State*)screen;
+    rc = ensure_slab(this, S, nq);
+    if (rc != CT_OK) return rc;
+    cudaError_t e = cudaStreamWaitEvent(st, S->slab_done, 0);
+    const size_t n0 = (size_t)n;
+    long long* ids = nullptr;
+    int* scratch = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&ids, sizeof(long long) * nq, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&scratch, sizeof(int) * nq, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(vnat + n0 * m, qv, sizeof(float) * nq * m, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(coords_raw + n0 * d, qcoords, sizeof(float) * nq * d, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(p + n0, qp, sizeof(float) * nq, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+        scale_rows_kernel<<<grid_for(nq * d), 256, 0, st>>>(qcoords, nq, d, inv_ls, xs + n0 * d);
+        point_scalars_kernel<<<grid_for(nq), 256, 0, st>>>(vnat + n0 * m, p + n0, xs + n0 * d, nq, m, d,
+                                                         S->vn + n0, S->isp + n0, S->xmax + n0);
+        iota64_kernel<<<grid_for(nq), 256, 0, st>>>(ids, nq, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = ct::hilbert_keys_bounded(qcoords, nq, d, S->bounds, S->hil_key + n0, scratch, st);
+    if (e != cudaSuccess) {
+        cudaFreeAsync(ids, st); cudaFreeAsync(scratch, st);
+        return set_err(CT_ERR_CUDA, "screened points: slab fill: %s", cudaGetErrorString(e));
+    }
+    rc = knn_screened((const int64_t*)ids, nq, k, 0, out_idx, out_dist, stats, st, n + nq);
+    cudaFreeAsync(ids, st);
+    cudaFreeAsync(scratch, st);
+    cudaEventRecord(S->slab_done, st);
+    if (stats && rc == CT_OK) stats->kernel_launches += 4;
+    return rc;
 }
 
 // Diagnostic: raw screened dot products of 128 query rows x 256 candidate rows.

@@ -52,8 +52,11 @@ struct ct_tree {
     int build_tree(const float* v_dataset, const float* coords_dataset, cudaStream_t st);
     int knn_tree(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
                  ct_stats* stats, cudaStream_t st);
+    // id_limit: query ids must lie in [0, id_limit) (default n; rows >= n are the query slab)
     int knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
-                     ct_stats* stats, cudaStream_t st);
+                     ct_stats* stats, cudaStream_t st, long long id_limit = -1);
+    int knn_screened_points(const float* qv, const float* qp, const float* qcoords, int64_t nq, int k,
+                            int64_t* out_idx, float* out_dist, ct_stats* stats, cudaStream_t st);
     void release_screen();
     ~ct_tree();
 

@@ -109,9 +109,10 @@ class CudaResidualIndex:
         idx, dist = self.knn_device(q, k, predecessor=predecessor, form=form)
         return idx.cpu().numpy(), dist.cpu().numpy()
 
-    def knn_points_device(self, qv, qp, qcoords, k: int, *, stream=None, out=None):
+    def knn_points_device(self, qv, qp, qcoords, k: int, *, form: str = "dense", stream=None, out=None):
         """kNN of NEW points: V rows qv [Q,m] (e.g. from CudaVFactor.embed_device), p values
-        qp [Q] and raw coordinates qcoords [Q,d].  Returns (idx, dist) CUDA tensors."""
+        qp [Q] and raw coordinates qcoords [Q,d].  form: "dense" (plain FP32) or
+        "screened".  Returns (idx, dist) CUDA tensors."""
         torch = _torch()
         qv = _as_device(qv, torch.float32, self.device)
         qp = _as_device(qp, torch.float32, self.device).reshape(-1)
@@ -126,8 +127,8 @@ class CudaResidualIndex:
             idx, dist = out
         st = _lib.CtStats()
         _lib.check(_lib.load().ct_knn_residual_points(self._h, qv.data_ptr(), qp.data_ptr(), qc.data_ptr(), nq, k,
-                                                      idx.data_ptr(), dist.data_ptr(), ctypes.byref(st),
-                                                      _stream_ptr(stream)))
+                                                      _lib.FORMS[form], idx.data_ptr(), dist.data_ptr(),
+                                                      ctypes.byref(st), _stream_ptr(stream)))
         self.last_stats = st.as_dict()
         return idx, dist
 

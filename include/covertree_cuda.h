@@ -166,11 +166,16 @@ CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d
  * k nearest dataset rows of NEW points (no counterpart in the reference, whose
  * queries are dataset ids only).  Query row i is qv[i] [m] (natural column order,
  * as ct_vfactor_embed writes it), qp[i] and qcoords[i] [d] (unscaled); all device f32.
- * Each point is scaled, normalised and compared exactly like one more dataset row
- * would be (plain FP32, the dense form's arithmetic).  k <= 128.
+ * form CT_FORM_DENSE: each point is scaled, normalised and compared exactly like one
+ * more dataset row would be (plain FP32, the dense form's arithmetic), k <= 128.
+ * form CT_FORM_SCREENED: BF16 tcgen05 screening + FP64-grade rescoring (the screened
+ * form's contract), k <= 64, d <= 8; the points pass through a per-tree query slab
+ * (grown on demand, which synchronises the device), and calls on one tree take turns.
+ * Either way a point's result does not depend on the other points of the call.
  */
 CT_API int ct_knn_residual_points(ct_tree* tree, const float* qv, const float* qp, const float* qcoords, int64_t nq,
-                                  int32_t k, int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream);
+                                  int32_t k, int32_t form, int64_t* out_idx, float* out_dist, ct_stats* stats,
+                                  void* stream);
 
 /*
  * Batching form: many query sets against many resident trees in ONE persistent

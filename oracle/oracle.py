@@ -172,9 +172,10 @@ def residual_dist_f64(V, p, coords, var, ls, kernel_type, qi, cj):
     return d
 
 
-def brute_knn_f64(V, p, coords, var, ls, kernel_type, queries, k, predecessor, block=256):
-    """Exact kNN in FP64, ascending by (dist, idx); -1 / +inf padding.  Returns (idx, dist)."""
-    n = V.shape[0]
+def brute_knn_f64(V, p, coords, var, ls, kernel_type, queries, k, predecessor, block=256, cand_limit=None):
+    """Exact kNN in FP64, ascending by (dist, idx); -1 / +inf padding.  Returns (idx, dist).
+    cand_limit: candidates are rows [0, cand_limit) (rows beyond hold new query points)."""
+    n = V.shape[0] if cand_limit is None else int(cand_limit)
     queries = np.asarray(queries, dtype=np.int64)
     out_i = np.full((queries.size, k), -1, dtype=np.int64)
     out_d = np.full((queries.size, k), np.inf, dtype=np.float64)

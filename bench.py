@@ -47,6 +47,10 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=2048, help="queries per CPU baseline sample")
     ap.add_argument("--n", type=int, default=None, help="override N of the workload (profiling on a smaller case)")
+    ap.add_argument("--no-batching", action="store_true", help="skip the 64-tree batching-form measurement")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
+    ap.add_argument("--serving-rates", default="100,500,1000", help="request rates (req/s) of the serving sweep")
+    ap.add_argument("--serving-seconds", type=float, default=2.0, help="arrival window per serving rate")
     return ap.parse_args()
 
 
@@ -182,6 +186,148 @@ def run_reference(args, wl):
         "build_seconds": build_s,
     }
     print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ batching form
+def fp32_core_peak(sm_mhz):
+    """Separately rounded FP32 multiply + add throughput of the CUDA cores (the plain
+    form's arithmetic): SMs x 128 lanes x clock, in T ops/s.  Computed, not measured."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = sm_mhz or 2070.0
+    return sms * 128 * mhz * 1e6 / 1e12
+
+
+def bench_batching(dev, steps: int = 3, warmup: int = 1):
+    """64 independent trees (N log-uniform [2048, 65536], D in {2,3,5}, Matern/RBF
+    alternating, m = 128, k in {10,30,50}, predecessor alternating), every point of
+    every tree queried: one persistent launch per step (CUDA-graph replay, autotuned
+    shape) against one dense launch per tree."""
+    import torch
+
+    from covertreex_gb300 import synthetic
+    from covertreex_gb300.device import CudaBatch, CudaResidualIndex, CudaVFactor
+    from covertreex_gb300.residual import inducing_indices
+
+    specs = synthetic.batch_trees()
+    trees = []
+    t0 = time.perf_counter()
+    for sp in specs:
+        X = synthetic.tree_coords(sp)
+        ind = inducing_indices(sp.n, sp.m, sp.inducing_seed)
+        f = CudaVFactor(X[ind].astype(np.float64), kernel_type=sp.kernel_type, variance=1.0,
+                        lengthscale=sp.lengthscale, device=dev)
+        V, p = f.embed_device(torch.as_tensor(X, device=dev))
+        index = CudaResidualIndex(V, p, X, variance=1.0, lengthscale=sp.lengthscale, kernel_type=sp.kernel_type,
+                                  build_tree=False, device=dev)
+        f.free()
+        del V, p
+        trees.append((sp, index, torch.arange(sp.n, dtype=torch.int64, device=dev)))
+    torch.cuda.synchronize(dev)
+    build_s = time.perf_counter() - t0
+    b = CudaBatch(dev)
+    outs = [b.add_ids(index, q, sp.k, predecessor=sp.predecessor) for sp, index, q in trees]
+    t1 = time.perf_counter()
+    shape = b.autotune(reps=1)
+    tune_s = time.perf_counter() - t1
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        b.run(use_graph=True)
+    torch.cuda.synchronize(dev)
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    ms = []
+    for _ in range(steps):
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        b.run(use_graph=True)
+        e.record(stream)
+        e.synchronize()
+        ms.append(a.elapsed_time(e))
+    clocks = sampler.stop()
+    got = [(i.clone(), d.clone()) for i, d in outs]
+    # per-tree form: one ct_knn_residual (dense) launch per tree, back to back
+    per = []
+    for _ in range(max(1, steps - 1)):
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for (sp, index, q), (i, d) in zip(trees, outs):
+            index.knn_device(q, sp.k, predecessor=sp.predecessor, form="dense", out=(i, d))
+        e.record(stream)
+        e.synchronize()
+        per.append(a.elapsed_time(e))
+    same = all(torch.equal(g[0], o[0]) and torch.equal(g[1], o[1]) for g, o in zip(got, outs))
+    nq = sum(sp.n for sp in specs)
+    pairs = sum(sp.n * sp.n * (0.5 if sp.predecessor else 1.0) for sp in specs)
+    macs = sum(sp.n * sp.n * (0.5 if sp.predecessor else 1.0) * sp.m for sp in specs)
+    step_ms = float(np.mean(ms))
+    peak = fp32_core_peak(clocks.get("sm_mhz"))
+    ops = 2.0 * macs / (step_ms / 1e3) / 1e12
+    for sp, index, q in trees:
+        index.free()
+    b.free()
+    return {
+        "workload": "64 trees: N log-uniform [2048, 65536], D in {2,3,5}, Matern 5/2 / RBF alternating, "
+                    "lengthscale U[0.5,2], m=128, k in {10,30,50}, predecessor alternating; all N ids queried",
+        "trees": len(specs), "queries": nq, "pairs": pairs,
+        "ms_per_step": step_ms, "queries_per_s": nq / (step_ms / 1e3),
+        "per_tree_launches": {"ms_per_step": float(np.mean(per)), "queries_per_s": nq / (np.mean(per) / 1e3),
+                              "launches_per_step": len(specs)},
+        "speedup_vs_per_tree": float(np.mean(per)) / step_ms,
+        "gpu_launches_per_step": 1, "cuda_graph": True, "shape": shape, "autotune_s": tune_s,
+        "identical_to_per_tree": bool(same), "setup_s": build_s, "dtype": "f32",
+        "roofline": {"bound": "fp32 cores (separately rounded multiply + add)", "achieved": ops, "peak": peak,
+                     "unit": "Tops/s", "frac": ops / peak,
+                     "peak_kind": "computed: SMs x 128 lanes x median SM clock (no measured FP32 peak)"},
+        "clocks": clocks,
+    }
+
+
+# ------------------------------------------------------------------ serving form
+def bench_serving(dev, rates, seconds: float):
+    """Poisson request streams (10% builds of N log-uniform [1k, 128k], D=3, Matern
+    5/2, m=256; 90% queries of 1..4096 new points, k in {30,50,60}) served with
+    continuous batching against a 120 GB HBM budget, beside the plain per-request form."""
+    from covertreex_gb300 import synthetic
+    from covertreex_gb300.serving import QueryRequest, ServingEngine, latency_summary
+
+    out = []
+    for rate in rates:
+        pre, stream = synthetic.serving_stream(rate, seconds, seed=6, preload=8)
+        warm = [QueryRequest(rid=10**7 + j, arrival=0.0, tree=pre[j % len(pre)].rid,
+                             points=np.random.default_rng(j).standard_normal((1 + 137 * j, 3)).astype(np.float32),
+                             k=(30, 50, 60)[j % 3]) for j in range(30)]
+        eng = ServingEngine(hbm_budget_bytes=120e9)
+        try:
+            eng.preload(pre)
+            eng.serve(warm, realtime=False)
+            l0 = eng.launches
+            t0 = time.perf_counter()
+            recs = eng.serve(stream, realtime=True, time_limit=4 * seconds + 2)
+            wall = time.perf_counter() - t0
+            row = {"rate_req_s": rate, "requests": len(stream), "wall_s": wall,
+                   "query": latency_summary(recs, "query"), "build": latency_summary(recs, "build"),
+                   "peak_hbm_GB": eng.peak_bytes / 1e9, "evicted": len(eng.evicted),
+                   "gpu_launches": eng.launches - l0}
+        finally:
+            eng.close()
+        if rate <= 500:
+            eng = ServingEngine(hbm_budget_bytes=120e9)
+            try:
+                eng.preload(pre)
+                eng.serve_per_request(warm, realtime=False)
+                base = eng.serve_per_request(stream, realtime=True, time_limit=4 * seconds + 2)
+                row["per_request"] = latency_summary(base, "query")
+                row["per_request"]["unfinished"] = len(stream) - len(base)
+            finally:
+                eng.close()
+        out.append(row)
+    return {"workload": "seeded Poisson stream (seed 6): 10% builds N log-uniform [1k,128k], D=3, Matern 5/2, "
+                        "lengthscale U[0.5,2], m=256; 90% queries of 1..4096 N(0,1) points (log-uniform), "
+                        "k in {30,50,60}; 8 trees preloaded",
+            "hbm_budget_GB": 120, "seconds_per_rate": seconds, "rates": out,
+            "p99_target_ms": 5.0}
 
 
 # ------------------------------------------------------------------ GPU leg
@@ -337,6 +483,20 @@ def main():
             cpu = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"unavailable: {exc}"}
 
+    batching = None
+    serving = None
+    if rank == 0 and world == 1 and not args.no_batching:
+        try:
+            batching = bench_batching(dev)
+        except Exception as exc:
+            batching = {"unavailable": repr(exc)}
+    if rank == 0 and world == 1 and not args.no_serving:
+        try:
+            serving = bench_serving(dev, [float(x) for x in args.serving_rates.split(",") if x],
+                                    args.serving_seconds)
+        except Exception as exc:
+            serving = {"unavailable": repr(exc)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -356,6 +516,8 @@ def main():
             "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,
             "neighbour_agreement_vs_plain": agree,
             "wall_s_timed": t_wall,
+            "batching": batching,
+            "serving": serving,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -50,6 +50,8 @@ EXPORTED_SYMBOLS = (
     "ct_vfactor_chol",
     "ct_vfactor_free",
     "ct_knn_residual_points",
+    "ct_prepare_screened",
+    "ct_tree_device_bytes",
     "ct_batch_create",
     "ct_batch_clear",
     "ct_batch_add_ids",
@@ -58,6 +60,7 @@ EXPORTED_SYMBOLS = (
     "ct_batch_autotune",
     "ct_batch_run",
     "ct_batch_get_shape",
+    "ct_batch_reserve",
     "ct_batch_free",
 )
 
@@ -142,6 +145,10 @@ def load(build_if_missing: bool = True):
         L.ct_vfactor_free.restype = ctypes.c_int
         L.ct_vfactor_free.argtypes = [vp]
         ip32 = ctypes.POINTER(i32)
+        L.ct_prepare_screened.restype = ctypes.c_int
+        L.ct_prepare_screened.argtypes = [vp, vp]
+        L.ct_tree_device_bytes.restype = ctypes.c_int
+        L.ct_tree_device_bytes.argtypes = [vp, ctypes.POINTER(i64)]
         L.ct_knn_residual_points.restype = ctypes.c_int
         L.ct_knn_residual_points.argtypes = [vp, vp, vp, vp, i64, i32, i32, vp, vp, ctypes.POINTER(CtStats), vp]
         L.ct_batch_create.restype = ctypes.c_int
@@ -160,6 +167,8 @@ def load(build_if_missing: bool = True):
         L.ct_batch_run.argtypes = [vp, i32, ctypes.POINTER(CtStats), vp]
         L.ct_batch_get_shape.restype = ctypes.c_int
         L.ct_batch_get_shape.argtypes = [vp, ip32, ip32, ip32, ip32, ctypes.POINTER(i64)]
+        L.ct_batch_reserve.restype = ctypes.c_int
+        L.ct_batch_reserve.argtypes = [vp, i32, i32, i32]
         L.ct_batch_free.restype = ctypes.c_int
         L.ct_batch_free.argtypes = [vp]
         _handle = L

@@ -38,6 +38,21 @@ int cuda_fail(cudaError_t e, const char* where) {
     return fail(CT_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
 }
 
+// The engine's per-call buffers come from the stream-ordered allocator; let the
+// device's default pool keep freed memory for reuse (this process only) instead of
+// returning it at every synchronisation.
+void keep_pool_memory() {
+    static bool done[64] = {false};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long keep = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    done[dev] = true;
+}
+
 }  // namespace
 
 namespace ct {
@@ -73,6 +88,7 @@ int ct_build_residual(const float* v, const float* p, const float* coords, int64
     if (!v || !p || !coords) return fail(CT_ERR_ARG, "ct_build_residual: NULL input pointer");
     if (kernel_type != CT_KERNEL_RBF && kernel_type != CT_KERNEL_MATERN52) kernel_type = CT_KERNEL_RBF;
     cudaStream_t st = (cudaStream_t)stream;
+    keep_pool_memory();
 
     ct_tree* T = new (std::nothrow) ct_tree();
     if (!T) return fail(CT_ERR_NOMEM, "ct_build_residual: host allocation failed");
@@ -213,6 +229,18 @@ int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* c
     return rc == CT_OK ? CT_OK : fail(rc, "ct_knn_residual_dense_noalloc: %s", msg);
 }
 
+int ct_prepare_screened(ct_tree* T, void* stream) {
+    if (!T) return fail(CT_ERR_ARG, "ct_prepare_screened: tree is NULL");
+    int rc = T->prepare_screened((cudaStream_t)stream);
+    return rc ? fail(rc, "ct_prepare_screened: %s", T->err) : CT_OK;
+}
+
+int ct_tree_device_bytes(const ct_tree* T, int64_t* bytes) {
+    if (!T || !bytes) return fail(CT_ERR_ARG, "ct_tree_device_bytes: NULL argument");
+    *bytes = T->device_bytes();
+    return CT_OK;
+}
+
 int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {
     if (!T) return fail(CT_ERR_ARG, "ct_tree_shape: tree is NULL");
     if (n) *n = T->n;
@@ -269,6 +297,7 @@ int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type
     if (!z) return fail(CT_ERR_ARG, "ct_vfactor_create: z is NULL");
     if (kernel_type != CT_KERNEL_RBF && kernel_type != CT_KERNEL_MATERN52) kernel_type = CT_KERNEL_RBF;
     cudaStream_t st = (cudaStream_t)stream;
+    keep_pool_memory();
     ct_vfactor* F = new (std::nothrow) ct_vfactor();
     if (!F) return fail(CT_ERR_NOMEM, "ct_vfactor_create: host allocation failed");
     F->m = m; F->d = d; F->kernel_type = kernel_type; F->variance = variance; F->lengthscale = lengthscale;
@@ -300,20 +329,18 @@ int ct_vfactor_embed(ct_vfactor* F, const double* x, int64_t n, float* v_out, fl
     if (n == 0) return CT_OK;
     if (!x || !v_out || !p_out) return fail(CT_ERR_ARG, "ct_vfactor_embed: NULL pointer");
     cudaStream_t st = (cudaStream_t)stream;
-    const long long want = ct::vmatrix_chunk_rows(n, F->m);
-    if (want > F->chunk) {
-        // grow the scratch; cudaFree waits for earlier embeds that still use it
-        if (F->kc) cudaFree(F->kc);
-        if (F->vc) cudaFree(F->vc);
-        F->kc = F->vc = nullptr;
-        F->chunk = 0;
-        CT_CUDA(cudaMalloc((void**)&F->kc, sizeof(double) * (size_t)want * F->m), "ct_vfactor_embed: scratch");
-        CT_CUDA(cudaMalloc((void**)&F->vc, sizeof(double) * (size_t)want * F->m), "ct_vfactor_embed: scratch");
-        F->chunk = want;
-    }
-    CT_CUDA(ct::vmatrix_embed(x, n, F->d, F->z, F->m, F->kernel_type, F->variance, F->lengthscale, F->Li, F->kc,
-                              F->vc, F->chunk, v_out, p_out, st, nullptr),
-            "ct_vfactor_embed launch");
+    // scratch is stream-ordered and private to the call: embeds on one factor may
+    // run concurrently on different streams (the factor itself is read-only)
+    const long long chunk = ct::vmatrix_chunk_rows(n, F->m);
+    double *kc = nullptr, *vc = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&kc, sizeof(double) * (size_t)chunk * F->m, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&vc, sizeof(double) * (size_t)chunk * F->m, st);
+    if (e == cudaSuccess)
+        e = ct::vmatrix_embed(x, n, F->d, F->z, F->m, F->kernel_type, F->variance, F->lengthscale, F->Li, kc, vc,
+                              chunk, v_out, p_out, st, nullptr);
+    if (kc) cudaFreeAsync(kc, st);
+    if (vc) cudaFreeAsync(vc, st);
+    if (e != cudaSuccess) return cuda_fail(e, "ct_vfactor_embed");
     return CT_OK;
 }
 
@@ -330,8 +357,6 @@ int ct_vfactor_free(ct_vfactor* F) {
     if (F->z) cudaFree(F->z);
     if (F->L) cudaFree(F->L);
     if (F->Li) cudaFree(F->Li);
-    if (F->kc) cudaFree(F->kc);
-    if (F->vc) cudaFree(F->vc);
     delete F;
     return CT_OK;
 }

@@ -49,7 +49,7 @@ struct Problem {
     long long* part_idx;  // [nq][split][k] partial lists (split > 1)
     float* part_dist;
     int* tile_done;       // [tiles] chunk completion counters (split > 1)
-    int split;            // candidate chunks per tile (1..32)
+    int split;            // candidate chunks per tile (1..kMaxSplit)
     int pad_;
 };
 
@@ -62,7 +62,9 @@ struct Header {
 constexpr size_t kHeaderBytes = 64;
 
 // Merge a tile's `split` sorted partial lists per query into the final top-k.
-// One warp per query; lane s holds the head of list s.
+// One warp per query; lane l owns lists l, l+32, l+64 and l+96 and offers the
+// smallest of their heads to a warp-wide (dist, idx) minimum.
+constexpr int kMaxSplit = 128;
 __device__ void merge_partials(const Problem& B, long long tile, int QT) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int k = B.base.k, S = B.split;
@@ -70,27 +72,32 @@ __device__ void merge_partials(const Problem& B, long long tile, int QT) {
     for (int qi = warp; qi < QT; qi += dense::kThreads / 32) {
         const long long g = tile * QT + qi;
         if (g >= B.base.nq) continue;
-        const long long* pi = B.part_idx + (g * S + lane) * k;
-        const float* pd = B.part_dist + (g * S + lane) * k;
-        int pos = 0;
-        float hd = kInf;
-        long long hi = LLONG_MAX;
-        auto load = [&]() {
-            hd = kInf;
-            hi = LLONG_MAX;
-            if (lane < S && pos < k) {
-                long long i = __ldcg(pi + pos);
-                if (i >= 0) { hi = i; hd = __ldcg(pd + pos); }
+        int pos[4] = {0, 0, 0, 0};
+        float hd[4];
+        long long hi[4];
+        auto load = [&](int h) {
+            const int list = lane + 32 * h;
+            hd[h] = kInf;
+            hi[h] = LLONG_MAX;
+            if (list < S && pos[h] < k) {
+                const long long off = (g * S + list) * k + pos[h];
+                const long long i = __ldcg(B.part_idx + off);
+                if (i >= 0) { hi[h] = i; hd[h] = __ldcg(B.part_dist + off); }
             }
         };
-        load();
+#pragma unroll
+        for (int h = 0; h < 4; ++h) load(h);
         for (int j = 0; j < k; ++j) {
-            float bd = hd;
-            long long bi = hi;
+            int bh = 0;
+#pragma unroll
+            for (int h = 1; h < 4; ++h)
+                if (nb_less(hd[h], hi[h], hd[bh], hi[bh])) bh = h;
+            float bd = hd[bh];
+            long long bi = hi[bh];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                float od = __shfl_xor_sync(0xffffffffu, bd, o);
-                long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+                const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (nb_less(od, oi, bd, bi)) { bd = od; bi = oi; }
             }
             if (lane == 0) {
@@ -98,7 +105,7 @@ __device__ void merge_partials(const Problem& B, long long tile, int QT) {
                 B.base.out_idx[g * k + j] = pad ? -1LL : bi;
                 B.base.out_dist[g * k + j] = pad ? CT_FLT_MAX : bd;
             }
-            if (bi != LLONG_MAX && hi == bi) { ++pos; load(); }
+            if (bi != LLONG_MAX && hi[bh] == bi) { ++pos[bh]; load(bh); }
         }
     }
 }
@@ -211,6 +218,7 @@ struct ct_batch {
     size_t smem_optin = 0, smem_per_sm = 0;
     std::vector<BatchReq> reqs;
     int cfg_qt = 0, cfg_cps = 0, cfg_ips = 0;  // 0 = automatic
+    int res_m = 16, res_d = 1, res_k = 1;      // shared memory is sized for at least these
     // device and pinned buffers
     unsigned char* d_desc = nullptr;
     unsigned char* h_desc = nullptr;
@@ -274,7 +282,7 @@ int batch_init(ct_batch* B) {
 constexpr size_t kStaticSmem = sizeof(dense::Tile) + 64;
 
 size_t smem_for(const ct_batch* B, int qt) {
-    int m = 16, d = 1, k = 1;
+    int m = B->res_m, d = B->res_d, k = B->res_k;
     for (const BatchReq& r : B->reqs) {
         m = std::max(m, r.tree->m);
         d = std::max(d, r.tree->d);
@@ -336,7 +344,7 @@ void make_plan(const ct_batch* B, int qt, int cps, int ips, Plan& P) {
         int split = 1;
         if ((double)total_tiles < target_items && total_work > 0) {
             const double want = target_items * (tile_work[i] * pr.tiles / total_work) / (double)pr.tiles;
-            split = (int)std::min(32.0, std::max(1.0, want));
+            split = (int)std::min((double)kMaxSplit, std::max(1.0, want));
         }
         long long chunk = (T->n + split - 1) / split;
         chunk = ((chunk + dense::kCT - 1) / dense::kCT) * dense::kCT;
@@ -434,7 +442,8 @@ int run_shape(ct_batch* B, int qt, int cps, int ips, bool use_graph, cudaStream_
     cudaError_t e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return B->cuda_err(e, "ct_batch: shared-memory attribute");
     long long grid = (long long)B->num_sms * cps;
-    if (grid > P.total_items) grid = P.total_items;
+    // a graph keeps one grid for every batch (CTAs without items leave at once)
+    if (!use_graph && grid > P.total_items) grid = P.total_items;
     B->last_grid = (int)grid;
 
     if (use_graph) {
@@ -474,10 +483,19 @@ void default_shape(const ct_batch* B, int& qt, int& cps, int& ips) {
     cps = B->cfg_cps > 0 ? B->cfg_cps : 1;
     ips = B->cfg_ips > 0 ? B->cfg_ips : 4;
     if (qt == 0) {
+        // the tile height whose padded work, weighted by the measured per-pair cost of
+        // the narrower tiles (more shared-memory traffic per multiply), is smallest
         const int order[3] = {64, 32, 16};
+        const double cost[3] = {1.0, 1.6, 2.6};
+        double best = -1.0;
         qt = 16;
-        for (int t = 0; t < 3; ++t)
-            if (shape_fits(B, order[t], 1)) { qt = order[t]; break; }
+        for (int t = 0; t < 3; ++t) {
+            if (!shape_fits(B, order[t], 1)) continue;
+            double w = 0.0;
+            for (const BatchReq& r : B->reqs)
+                w += (double)((r.nq + order[t] - 1) / order[t]) * order[t] * (double)r.tree->n * cost[t];
+            if (best < 0.0 || w < best) { best = w; qt = order[t]; }
+        }
     }
     if (!shape_fits(B, qt, cps)) cps = 1;
 }
@@ -552,6 +570,15 @@ int ct_batch_set_shape(ct_batch* B, int32_t qt, int32_t ctas_per_sm, int32_t ite
     if (items_per_slot < 0 || items_per_slot > 64)
         return ct::batch_fail("ct_batch_set_shape", "items_per_slot must be in [0, 64]", CT_ERR_ARG);
     B->cfg_qt = qt; B->cfg_cps = ctas_per_sm; B->cfg_ips = items_per_slot;
+    return CT_OK;
+}
+
+int ct_batch_reserve(ct_batch* B, int32_t m, int32_t d, int32_t k) {
+    if (!B) return ct::batch_fail("ct_batch_reserve", "batch is NULL", CT_ERR_ARG);
+    if (m < 16 || m % 16 != 0 || d < 1 || d > 64 || k < 1 || k > 128)
+        return ct::batch_fail("ct_batch_reserve", "need m a positive multiple of 16, 1 <= d <= 64, 1 <= k <= 128",
+                              CT_ERR_ARG);
+    B->res_m = m; B->res_d = d; B->res_k = k;
     return CT_OK;
 }
 

@@ -30,6 +30,7 @@
 // accumulation inside the tensor core (one rounding per MMA step plus the
 // step's internal alignment), both relative to sum |v_qi v_ci| <= ||v_q|| ||v_c||.
 #include <cuda_bf16.h>
+#include <limits.h>
 #include <string.h>
 
 #include <algorithm>
@@ -102,6 +103,8 @@ struct MMAParams {
     float* out_f;        // debug output
     int* surv; int* surv_cnt;
     int* status;
+    unsigned* qtau;      // per query (slot / parts): the smallest part threshold, float bits
+    int parts;           // candidate parts per query (slots s*parts .. s*parts+parts-1)
 };
 
 struct SmemLayout {
@@ -335,6 +338,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     const float t = __uint_as_float(~(unsigned)w);
                     if (t < tau2) { tau2 = t; thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq; }
                 }
+                // the other parts' thresholds of this query (any part's k-th upper
+                // bound bounds the query's k-th distance)
+                const float tg = __uint_as_float(__ldcg(&P.qtau[slot / P.parts]));
+                if (tg < tau2) { tau2 = tg; thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq; }
             }
             for (int cc = 0; cc < 16; ++cc) {
                 float v[8];
@@ -401,6 +408,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                                 thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq;
                                 atomicMax(&rowtau[row], ((unsigned long long)gen << 32) |
                                                             (unsigned long long)(~__float_as_uint(tau2)));
+                                if (P.parts > 1) atomicMin(&P.qtau[slot / P.parts], __float_as_uint(tau2));
                             }
                         }
                     }
@@ -876,6 +884,83 @@ __global__ void arows_kernel(const int* sorted_slots, long long nq, long long ro
     rowmap[r] = id;
 }
 
+// Candidate parts: A row (t*parts + p)*TQ + r repeats A row t*TQ + r for part p,
+// whose slot is s*parts + p.
+__global__ void expand_parts_kernel(const int* a_slot, const int* rowmap, long long rows_q, int parts, int* a_slot_x,
+                                    int* rowmap_x) {
+    const long long r2 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r2 >= rows_q * parts) return;
+    const long long t2 = r2 / TQ;
+    const int r = (int)(r2 - t2 * TQ);
+    const long long t = t2 / parts;
+    const int pp = (int)(t2 - t * parts);
+    const long long r1 = t * TQ + r;
+    const int sl = a_slot[r1];
+    a_slot_x[r2] = sl >= 0 ? sl * parts + pp : -1;
+    rowmap_x[r2] = rowmap[r1];
+}
+__global__ void fill_u32_kernel(unsigned* a, long long n, unsigned v) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+__global__ void expand_slots_kernel(const int* slot_id, long long nq, int parts, int* slot_id_x) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < nq * parts) slot_id_x[i] = slot_id[i / parts];
+}
+// One warp per query: the exact top-k over its parts.  A part slot that overflowed
+// was rescored against every candidate, so its list is already the answer;
+// otherwise the parts cover disjoint candidates and their lists are k-way merged
+// (lane p holds the head of part p).
+__global__ void merge_parts_kernel(const long long* __restrict__ pidx, const float* __restrict__ pdist,
+                                   const int* __restrict__ surv_cnt, long long nq, int parts, int k,
+                                   long long* __restrict__ out_idx, float* __restrict__ out_dist) {
+    const long long q = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= nq) return;
+    int full = -1;
+    for (int pp = 0; pp < parts; ++pp) {
+        const long long sl = q * parts + pp;
+        if (surv_cnt[2 * sl] > HALF_CAP || surv_cnt[2 * sl + 1] > HALF_CAP) { full = pp; break; }
+    }
+    if (full >= 0) {
+        const long long sl = q * parts + full;
+        for (int j = lane; j < k; j += 32) {
+            out_idx[q * k + j] = pidx[sl * k + j];
+            out_dist[q * k + j] = pdist[sl * k + j];
+        }
+        return;
+    }
+    const float kInf = __int_as_float(0x7f800000);
+    int pos = 0;
+    float hd = kInf;
+    long long hi = LLONG_MAX;
+    auto load = [&]() {
+        hd = kInf;
+        hi = LLONG_MAX;
+        if (lane < parts && pos < k) {
+            const long long i = pidx[(q * parts + lane) * k + pos];
+            if (i >= 0) { hi = i; hd = pdist[(q * parts + lane) * k + pos]; }
+        }
+    };
+    load();
+    for (int j = 0; j < k; ++j) {
+        float bd = hd;
+        long long bi = hi;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+            const long long oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (od < bd || (od == bd && oi < bi)) { bd = od; bi = oi; }
+        }
+        if (lane == 0) {
+            const bool pad = bi == LLONG_MAX;
+            out_idx[q * k + j] = pad ? -1LL : bi;
+            out_dist[q * k + j] = pad ? CT_FLT_MAX : bd;
+        }
+        if (bi != LLONG_MAX && hi == bi) { ++pos; load(); }
+    }
+}
+
 static inline unsigned grid_for(long long n, int b = 256) { return (unsigned)((n + b - 1) / b); }
 
 static float err_coef_for(int m) {
@@ -1030,9 +1115,13 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     unsigned long long *key_lvl = nullptr, *ktmp = nullptr;
     unsigned* hist = nullptr;
     int *a_slot_lvl = nullptr, *rowmap_lvl = nullptr;
+    int *a_slot_x = nullptr, *rowmap_x = nullptr, *slot_id_x = nullptr;  // part-expanded (parts > 1)
     bf16 *al_hi = nullptr, *al_lo = nullptr;
     int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr, *cta_begin = nullptr;
+    long long* part_idx = nullptr;
+    float* part_dist = nullptr;
     long long* evals_d = nullptr;
+    unsigned* qtau = nullptr;
     Job* jobs = nullptr;
     const int nbh = ct::radix_num_blocks(nq);
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes ? bytes : 16, st); };
@@ -1042,13 +1131,12 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     A((void**)&hist, sizeof(unsigned) * 256 * (size_t)nbh);
     A((void**)&a_slot_lvl, sizeof(int) * rows_q);
     A((void**)&rowmap_lvl, sizeof(int) * rows_q);
-    A((void**)&al_hi, sizeof(bf16) * rows_q * m); A((void**)&al_lo, sizeof(bf16) * rows_q * m);
-    A((void**)&surv, sizeof(int) * nq * SURV_CAP);
-    A((void**)&surv_cnt, sizeof(int) * 2 * nq);
-    A((void**)&full_list, sizeof(int) * nq);
     A((void**)&nfull_d, sizeof(int));
     A((void**)&evals_d, sizeof(long long));
+    A((void**)&qtau, sizeof(unsigned) * nq);
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
+    fill_u32_kernel<<<grid_for(nq), 256, 0, st>>>(qtau, nq, 0x3f800000u);  // tau^2 = 1
+    ++launches;
 
     slot_ids_kernel<<<grid_for(nq), 256, 0, st>>>((const long long*)q_ids, nq, id_limit > 0 ? id_limit : n,
                                                  slot_id, key_lvl, val_lvl,
@@ -1062,7 +1150,6 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         if (e == cudaSuccess) e = cudaMemcpyAsync(key_lvl, ktmp, 8 * nq, cudaMemcpyDeviceToDevice, st); }
     if (e == cudaSuccess) {
         arows_kernel<<<grid_for(rows_q), 256, 0, st>>>(val_lvl, nq, rows_q, slot_id, a_slot_lvl, rowmap_lvl);
-        split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_lvl, rows_q, al_hi, al_lo);
         e = cudaGetLastError();
     }
     std::vector<unsigned long long> hk_lvl(nq);
@@ -1096,15 +1183,11 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             const Level& L = S->levels[li];
             const long long t0 = L.row_off / TC, ntl = L.rows_pad / TC;
             const long long cc = std::min(std::max(row / TC, t0), t0 + ntl - 1);
-            std::vector<int> spiral;
-            spiral.push_back((int)cc);
+            J.push_back(Job{(int)t, (int)cc, 0, 0});
             for (long long dlt = 1; dlt < ntl; ++dlt) {
-                if (cc + dlt < t0 + ntl) spiral.push_back((int)(cc + dlt));
-                if (cc - dlt >= t0) spiral.push_back((int)(cc - dlt));
+                if (cc + dlt < t0 + ntl) J.push_back(Job{(int)t, (int)(cc + dlt), 0, 0});
+                if (cc - dlt >= t0) J.push_back(Job{(int)t, (int)(cc - dlt), 0, 0});
             }
-            const int warm = (int)std::min<size_t>(kWarmTiles, spiral.size());
-            for (int w = 0; w < warm; ++w) J.push_back(Job{(int)t, spiral[w], 2, 0});
-            for (size_t w = 0; w < spiral.size(); ++w) J.push_back(Job{(int)t, spiral[w], (int)w < warm ? 4 : 0, 0});
         }
         if (predecessor) {
             // ids >= the level size are not in the level: sweep them in dataset order
@@ -1112,15 +1195,50 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             long long hi_tile = std::min((maxq + TC - 1) / TC, n_ds_tiles);
             for (long long c = lo_tile; c < hi_tile; ++c) J.push_back(Job{(int)t, (int)c, 1, 0});
         }
-        if (!J.empty()) J[0].first = 1;
     }
-    // longest-processing-time assignment of query tiles to persistent CTAs
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // Candidate parts: with fewer query tiles than SMs, each query tile's candidate
+    // tiles are dealt round-robin into `parts` disjoint parts, each searched as its own
+    // slot (own A rows, heap and survivor lists); the parts' exact top-k lists are
+    // merged at the end.  A part's threshold bounds the k-th distance within the
+    // part, so its survivors still contain the part's true top k.
+    long long busy_tiles = 0, max_jobs = 0;
+    for (const auto& J : tiles) if (!J.empty()) { ++busy_tiles; max_jobs = std::max<long long>(max_jobs, (long long)J.size()); }
+    int parts = 1;
+    if (busy_tiles > 0 && busy_tiles < sms) {
+        parts = (int)std::min<long long>(32, sms / busy_tiles);
+        parts = (int)std::max<long long>(1, std::min<long long>(parts, max_jobs / 8));
+    }
+    const long long nslots = nq * parts;
+    const long long rows_x = rows_q * parts;
+    // jobs of each (query tile, part): a heap-only warm-up over the part's first tiles,
+    // then every tile of the part with survivors kept
+    std::vector<std::vector<Job>> ptiles(nqt * parts);
+    for (long long t = 0; t < nqt; ++t) {
+        const std::vector<Job>& J = tiles[t];
+        if (J.empty()) continue;
+        for (int pp = 0; pp < parts; ++pp) {
+            std::vector<Job> mine;
+            for (size_t w = pp; w < J.size(); w += parts) mine.push_back(J[w]);
+            if (mine.empty()) continue;
+            const int qt = (int)(t * parts + pp);
+            std::vector<Job>& out = ptiles[qt];
+            size_t nlevel_jobs = 0;
+            for (const Job& jb : mine) if (!(jb.which & 1)) ++nlevel_jobs;
+            const int warm = (int)std::min<size_t>(parts > 1 ? std::max<size_t>(1, std::min<size_t>(kWarmTiles, nlevel_jobs / 4))
+                                                             : kWarmTiles, nlevel_jobs);
+            for (int w = 0; w < warm; ++w) out.push_back(Job{qt, mine[w].ctile, 2, 0});
+            for (size_t w = 0; w < mine.size(); ++w)
+                out.push_back(Job{qt, mine[w].ctile, mine[w].which | ((int)w < warm ? 4 : 0), 0});
+            out[0].first = 1;
+        }
+    }
+    // longest-processing-time assignment of (query tile, part) units to persistent CTAs
     std::vector<long long> order;
-    for (long long t = 0; t < nqt; ++t) if (!tiles[t].empty()) order.push_back(t);
-    std::sort(order.begin(), order.end(), [&](long long a, long long b) { return tiles[a].size() > tiles[b].size(); });
+    for (long long t = 0; t < (long long)ptiles.size(); ++t) if (!ptiles[t].empty()) order.push_back(t);
+    std::sort(order.begin(), order.end(), [&](long long a, long long b) { return ptiles[a].size() > ptiles[b].size(); });
     const int ncta = (int)std::min<long long>((long long)sms, (long long)order.size());
     std::vector<std::vector<long long>> per_cta(ncta);
     std::vector<std::pair<long long, int>> load;  // (jobs, cta) min-heap
@@ -1131,22 +1249,47 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         std::pop_heap(load.begin(), load.end(), cmp);
         auto& lc = load.back();
         per_cta[lc.second].push_back(t);
-        lc.first += (long long)tiles[t].size();
+        lc.first += (long long)ptiles[t].size();
         std::push_heap(load.begin(), load.end(), cmp);
     }
     std::vector<Job> flat;
     std::vector<int> begin(ncta + 1, 0);
     for (int c = 0; c < ncta; ++c) {
         begin[c] = (int)flat.size();
-        for (long long t : per_cta[c]) flat.insert(flat.end(), tiles[t].begin(), tiles[t].end());
+        for (long long t : per_cta[c]) flat.insert(flat.end(), ptiles[t].begin(), ptiles[t].end());
     }
     begin[ncta] = (int)flat.size();
-    long long pairs_main = (long long)flat.size() * TQ * TC;
+    const long long pairs_main = (long long)flat.size() * TQ * TC;  // every job runs its MMAs
+    // part-expanded slots and A rows, the A operand, survivor lists
+    const int* a_slot_use = a_slot_lvl;
+    const int* rowmap_use = rowmap_lvl;
+    const int* slot_id_use = slot_id;
+    if (parts > 1) {
+        A((void**)&a_slot_x, sizeof(int) * rows_x);
+        A((void**)&rowmap_x, sizeof(int) * rows_x);
+        A((void**)&slot_id_x, sizeof(int) * nslots);
+        A((void**)&part_idx, sizeof(long long) * nslots * k);
+        A((void**)&part_dist, sizeof(float) * nslots * k);
+        if (e == cudaSuccess) {
+            expand_parts_kernel<<<grid_for(rows_x), 256, 0, st>>>(a_slot_lvl, rowmap_lvl, rows_q, parts, a_slot_x, rowmap_x);
+            expand_slots_kernel<<<grid_for(nslots), 256, 0, st>>>(slot_id, nq, parts, slot_id_x);
+            e = cudaGetLastError();
+            launches += 2;
+        }
+        a_slot_use = a_slot_x; rowmap_use = rowmap_x; slot_id_use = slot_id_x;
+    }
+    A((void**)&al_hi, sizeof(bf16) * rows_x * m); A((void**)&al_lo, sizeof(bf16) * rows_x * m);
+    A((void**)&surv, sizeof(int) * nslots * SURV_CAP);
+    A((void**)&surv_cnt, sizeof(int) * 2 * nslots);
+    A((void**)&full_list, sizeof(int) * nslots);
     A((void**)&jobs, sizeof(Job) * (flat.size() + 1));
     A((void**)&cta_begin, sizeof(int) * (ncta + 1));
+    if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
+    split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_use, rows_x, al_hi, al_lo);
+    ++launches;
     if (e == cudaSuccess && !flat.empty()) e = cudaMemcpyAsync(jobs, flat.data(), sizeof(Job) * flat.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(cta_begin, begin.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * 2 * nq, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * 2 * nslots, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(nfull_d, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(evals_d, 0, sizeof(long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(int), st);
@@ -1154,29 +1297,33 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (timing) cudaEventRecord(ev[1], st);
     if (timing) cudaEventRecord(ev[2], st);
     MMAParams P{};
-    P.a_hi = al_hi; P.a_lo = al_lo; P.a_groups = rows_q / 8;
+    P.a_hi = al_hi; P.a_lo = al_lo; P.a_groups = rows_x / 8;
     P.b_hi[0] = S->lvl_hi; P.b_lo[0] = S->lvl_lo; P.b_groups[0] = S->lvl_rows / 8; P.b_id[0] = S->lvl_id;
     P.b_hi[1] = S->ds_hi; P.b_lo[1] = S->ds_lo; P.b_groups[1] = S->rows_pad / 8; P.b_id[1] = S->b_id_ds;
     P.m = m; P.jobs = jobs; P.cta_job_begin = cta_begin;
-    P.a_slot = a_slot_lvl; P.slot_id = slot_id;
+    P.a_slot = a_slot_use; P.slot_id = slot_id_use;
     P.xs = xs; P.d = d; P.vn = S->vn; P.isp = S->isp; P.xmax = S->xmax;
     P.var = var; P.kernel_type = kernel_type; P.predecessor = predecessor ? 1 : 0;
     P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
     P.surv = surv; P.surv_cnt = surv_cnt; P.status = S->status;
+    P.qtau = qtau; P.parts = parts;
     if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
     if (timing) cudaEventRecord(ev[3], st);
-    // ---- rescoring
+    // ---- rescoring (into the part lists when parts > 1)
     RescoreParams R{};
     R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls = S->inv_ls64; R.p = p;
     R.var = (double)var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
-    R.slot_id = slot_id; R.nslots = nq; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list; R.nfull = 0;
-    R.k = k; R.out_idx = (long long*)out_idx; R.out_dist = out_dist; R.evals = evals_d;
+    R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list;
+    R.nfull = 0;
+    R.k = k; R.evals = evals_d;
+    R.out_idx = parts > 1 ? part_idx : (long long*)out_idx;
+    R.out_dist = parts > 1 ? part_dist : out_dist;
     const int rwpb = 8;
     const size_t rsmem = sizeof(unsigned long long) * RBUF * rwpb;
     if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
     if (e == cudaSuccess) {
-        rescore_kernel<<<(unsigned)((nq + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 0);
-        collect_overflow_kernel<<<grid_for(nq), 256, 0, st>>>(surv_cnt, nq, full_list, nfull_d);
+        rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 0);
+        collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, full_list, nfull_d);
         e = cudaGetLastError();
         launches += 2;
     }
@@ -1188,10 +1335,10 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     int* item_begin_d = nullptr;
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess && nfull > 0) {
-        // split every overflowed query's exhaustive range into chunks
-        std::vector<int> fl(nfull), sid(nq);
+        // split every overflowed slot's exhaustive range into chunks
+        std::vector<int> fl(nfull), sid(nslots);
         e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id, sizeof(int) * nq, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id_use, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         std::sort(fl.begin(), fl.end());
         std::vector<ChunkItem> items;
@@ -1221,6 +1368,12 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         // (host vectors stay alive until the synchronisation below)
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
+    if (e == cudaSuccess && parts > 1) {
+        merge_parts_kernel<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(part_idx, part_dist, surv_cnt, nq, parts, k,
+                                                                     (long long*)out_idx, out_dist);
+        e = cudaGetLastError();
+        ++launches;
+    }
     float ms_total = 0.f, ms_a = 0.f, ms_b = 0.f, ms_r = 0.f;
     if (timing && e == cudaSuccess) {
         cudaEventRecord(ev[4], st);
@@ -1244,7 +1397,12 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     cudaFreeAsync(al_hi, st); cudaFreeAsync(al_lo, st);
     cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
-    cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st);
+    cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st); cudaFreeAsync(qtau, st);
+    if (a_slot_x) cudaFreeAsync(a_slot_x, st);
+    if (rowmap_x) cudaFreeAsync(rowmap_x, st);
+    if (slot_id_x) cudaFreeAsync(slot_id_x, st);
+    if (part_idx) cudaFreeAsync(part_idx, st);
+    if (part_dist) cudaFreeAsync(part_dist, st);
     if (items_d) cudaFreeAsync(items_d, st);
     if (item_begin_d) cudaFreeAsync(item_begin_d, st);
     if (partial) cudaFreeAsync(partial, st);
@@ -1263,6 +1421,20 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         stats->overflow_queries = nfull;
     }
     return CT_OK;
+}
+
+// Device bytes of the metric arrays, the cover tree and the screened operands.
+long long ct_tree::device_bytes() const {
+    const long long rows = n + (screen ? ((const State*)screen)->slab_cap : 0);
+    long long b = (long long)n * m * 4 + n * (long long)d * 4 + n * 8 + 64 * 4;  // vperm, xs (dataset part), norms, p
+    b += rows * (long long)m * 4 + rows * (long long)d * 8 + rows * 4;           // vnat, coords_raw + slab xs, slab p
+    if (has_tree) b += n * (8 * 6 + 4 + 4) + (long long)n * (m + d + 2) * 4;
+    if (screen) {
+        const State* S = (const State*)screen;
+        b += S->rows_pad * (long long)m * 4 + S->lvl_rows * (long long)m * 4;   // hi + lo BF16 operands
+        b += S->rows_pad * 4 + S->lvl_rows * 12 + n * 12 + rows * 20 + 1024;
+    }
+    return b;
 }
 
 // ---------------------------------------------------------------- new points
@@ -1312,6 +1484,15 @@ int ensure_slab(ct_tree* T, State* S, long long rows) {
 }
 
 }  // namespace
+
+// Build the screened operands and a query slab of 4096 rows ahead of the first query.
+int ct_tree::prepare_screened(cudaStream_t st) {
+    if (m % KC != 0 || m > 1024) return set_err(CT_ERR_UNSUPPORTED, "screened form needs m %% 32 == 0 and m <= 1024 (got %d)", m);
+    if (d > kMaxD) return set_err(CT_ERR_UNSUPPORTED, "screened form supports d <= %d (got %d)", kMaxD, d);
+    int rc = screen_prepare(this, st);
+    if (rc == CT_OK) rc = ensure_slab(this, (State*)screen, 4096);
+    return rc;
+}
 
 // kNN of new points with the screened form: the points are written to the query
 // slab (rows n .. n+nq-1, with the dataset's own scaling, scalars and Hilbert

@@ -57,6 +57,8 @@ struct ct_tree {
                      ct_stats* stats, cudaStream_t st, long long id_limit = -1);
     int knn_screened_points(const float* qv, const float* qp, const float* qcoords, int64_t nq, int k,
                             int64_t* out_idx, float* out_dist, ct_stats* stats, cudaStream_t st);
+    int prepare_screened(cudaStream_t st);  // build the screened form's operands now
+    long long device_bytes() const;          // device memory held by the handle
     void release_screen();
     ~ct_tree();
 

@@ -10,7 +10,8 @@ namespace ct {
 cudaError_t vmatrix_factor(const double* z, int m, int d, int kt, double var, double ls, double* L, double* Li,
                            int* status_dev, cudaStream_t st);
 
-// Rows per chunk of the embed step (scratch kc and vc hold chunk x m doubles each).
+// Rows per chunk of the embed step (scratch kc and vc hold chunk x m doubles each;
+// at most about 256 MB each).
 long long vmatrix_chunk_rows(long long n, int m);
 
 // V [n x m] f32 and p [n] f32 for points x [n x d] (device FP64).
@@ -27,7 +28,4 @@ struct ct_vfactor {
     double* z = nullptr;   // m x d inducing points
     double* L = nullptr;   // m x m Cholesky factor (lower)
     double* Li = nullptr;  // m x m inverse of L (lower)
-    double* kc = nullptr;  // embed scratch: chunk x m
-    double* vc = nullptr;  // embed scratch: chunk x m
-    long long chunk = 0;   // rows the scratch holds
 };

@@ -132,6 +132,15 @@ class CudaResidualIndex:
         self.last_stats = st.as_dict()
         return idx, dist
 
+    def prepare_screened(self, stream=None):
+        """Build the screened form's BF16 operands now (otherwise done by the first screened query)."""
+        _lib.check(_lib.load().ct_prepare_screened(self._h, _stream_ptr(stream)))
+
+    def device_bytes(self) -> int:
+        b = ctypes.c_int64()
+        _lib.check(_lib.load().ct_tree_device_bytes(self._h, ctypes.byref(b)))
+        return int(b.value)
+
     def debug_screen_dots(self, rows_a, rows_b):
         """Raw BF16-screened dot products (hi.hi + hi.lo + lo.hi) of 128 x 256 dataset rows."""
         torch = _torch()
@@ -222,6 +231,10 @@ class CudaBatch:
     def set_shape(self, qt: int = 0, ctas_per_sm: int = 0, items_per_slot: int = 0):
         _lib.check(_lib.load().ct_batch_set_shape(self._h, int(qt), int(ctas_per_sm), int(items_per_slot)))
 
+    def reserve(self, m: int, d: int, k: int):
+        """Size the launch for at least (m, d, k) so varying mixes reuse one shape and graph."""
+        _lib.check(_lib.load().ct_batch_reserve(self._h, int(m), int(d), int(k)))
+
     def autotune(self, reps: int = 1, stream=None):
         q, c, i = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
         _lib.check(_lib.load().ct_batch_autotune(self._h, int(reps), _stream_ptr(stream), ctypes.byref(q),
@@ -304,6 +317,9 @@ class CudaVFactor:
     def embed(self, x):
         v, p = self.embed_device(x)
         return v.cpu().numpy(), p.cpu().numpy()
+
+    def device_bytes(self) -> int:
+        return 8 * (self.m * self.d + 2 * self.m * self.m)
 
     def chol(self) -> np.ndarray:
         torch = _torch()

@@ -78,3 +78,87 @@ def make(name: str, *, n: int | None = None) -> Workload:
     hb = build_residual_backend(X, seed=42, inducing_count=m, variance=1.0, lengthscale=ls, kernel_type=kt)
     return Workload(name=name, coords=X, v=hb.v_matrix, p=hb.p_diag, variance=1.0, lengthscale=ls, kernel_type=kt,
                     k=k, predecessor=pred)
+
+
+# ---------------------------------------------------------------------------
+# Batching workload: 64 independent trees of uneven N, D and k
+# ---------------------------------------------------------------------------
+@dataclass
+class TreeSpec:
+    n: int
+    d: int
+    kernel_type: int
+    lengthscale: float
+    m: int
+    k: int
+    predecessor: bool
+    coord_seed: int
+    inducing_seed: int
+
+
+def batch_trees(count: int = 64, seed: int = 5, n_min: int = 2048, n_max: int = 65536, m: int = 128):
+    """64 trees: N log-uniform in [2048, 65536], D in {2, 3, 5}, kernels alternating
+    Matern 5/2 / RBF, lengthscale U[0.5, 2], m = 128, k in {10, 30, 50}, predecessor
+    mode alternating.  Coordinates are N(0,1) float32 drawn per tree."""
+    r = np.random.default_rng(seed)
+    out = []
+    for t in range(count):
+        n = int(np.floor(np.exp(r.uniform(np.log(n_min), np.log(n_max)))))
+        d = int(r.choice([2, 3, 5]))
+        ls = float(r.uniform(0.5, 2.0))
+        k = int(r.choice([10, 30, 50]))
+        out.append(TreeSpec(n=n, d=d, kernel_type=1 if t % 2 == 0 else 0, lengthscale=ls, m=m, k=k,
+                            predecessor=(t % 2 == 1), coord_seed=seed * 1000 + t, inducing_seed=seed * 1000 + 500 + t))
+    return out
+
+
+def tree_coords(spec: TreeSpec) -> np.ndarray:
+    return np.random.default_rng(spec.coord_seed).standard_normal((spec.n, spec.d)).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Serving workload: a seeded Poisson stream of build and query requests
+# ---------------------------------------------------------------------------
+def serving_stream(rate: float, duration: float, *, seed: int = 6, preload: int = 8, build_frac: float = 0.1,
+                   n_min: int = 1024, n_max: int = 131072, m: int = 256, q_max: int = 4096,
+                   ks=(30, 50, 60), working_set: int = 32):
+    """Returns (preload_builds, stream).  Arrivals are Poisson at `rate` requests/s
+    over `duration` seconds.  Builds (fraction `build_frac`): N log-uniform in
+    [1k, 128k], D = 3, N(0,1) coordinates, Matern 5/2 with lengthscale U[0.5, 2],
+    m = 256.  Queries: 1..4096 new N(0,1) points (log-uniform count), k drawn from
+    {30, 50, 60}, against a tree drawn from the most recent `working_set` builds."""
+    from .serving import BuildRequest, QueryRequest
+
+    r = np.random.default_rng(seed)
+    rid = 0
+    builds = []
+
+    def make_build(arrival):
+        nonlocal rid
+        n = int(np.floor(np.exp(r.uniform(np.log(n_min), np.log(n_max)))))
+        cs = int(r.integers(0, 2**31 - 1))
+        X = np.random.default_rng(cs).standard_normal((n, 3)).astype(np.float32)
+        b = BuildRequest(rid=rid, arrival=arrival, coords=X, kernel_type=1, lengthscale=float(r.uniform(0.5, 2.0)),
+                         inducing_count=m, seed=cs % 100000)
+        rid += 1
+        return b
+
+    pre = [make_build(0.0) for _ in range(preload)]
+    recent = [b.rid for b in pre]
+    stream = []
+    t = 0.0
+    while True:
+        t += float(r.exponential(1.0 / rate))
+        if t > duration:
+            break
+        if r.random() < build_frac:
+            b = make_build(t)
+            stream.append(b)
+            recent = (recent + [b.rid])[-working_set:]
+        else:
+            q = int(np.clip(np.floor(np.exp(r.uniform(0.0, np.log(q_max)))), 1, q_max))
+            pts = r.standard_normal((q, 3)).astype(np.float32)
+            stream.append(QueryRequest(rid=rid, arrival=t, tree=int(r.choice(recent)), points=pts,
+                                       k=int(r.choice(ks))))
+            rid += 1
+    return pre, stream

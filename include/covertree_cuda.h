@@ -159,6 +159,13 @@ CT_API int ct_tree_arrays(const ct_tree* tree, int64_t* parents, int32_t* levels
 CT_API int ct_debug_screen_dots(ct_tree* tree, const int32_t* rows_a, const int32_t* rows_b, float* out,
                                 void* stream);
 
+/* Build the screened form's operands now instead of at the first screened query
+ * (synchronises `stream`).  No counterpart in the reference. */
+CT_API int ct_prepare_screened(ct_tree* tree, void* stream);
+
+/* Device memory held by a tree handle, in bytes (host output). */
+CT_API int ct_tree_device_bytes(const ct_tree* tree, int64_t* bytes);
+
 /* n, m, d of a tree (host outputs; any may be NULL). */
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
 
@@ -192,6 +199,8 @@ CT_API int ct_knn_residual_points(ct_tree* tree, const float* qv, const float* q
  *                        synchronising `stream`) and keep the fastest
  *   ct_batch_run         launch every added query set; asynchronous on `stream`
  *   ct_batch_get_shape   shape, grid and work-item count of the last run
+ *   ct_batch_reserve     size shared memory for at least (m, d, k), so that batches
+ *                        of different mixes keep one launch shape and one graph
  * Added query sets keep pointers to the caller's device buffers, which must stay
  * valid until the run completes.  Results do not depend on the shape or on the
  * other query sets of the batch.  One batch object serves one stream at a time.
@@ -209,6 +218,7 @@ CT_API int ct_batch_autotune(ct_batch* b, int32_t reps, void* stream, int32_t* q
 CT_API int ct_batch_run(ct_batch* b, int32_t use_graph, ct_stats* stats, void* stream);
 CT_API int ct_batch_get_shape(const ct_batch* b, int32_t* qt, int32_t* ctas_per_sm, int32_t* items_per_slot,
                               int32_t* grid, int64_t* items);
+CT_API int ct_batch_reserve(ct_batch* b, int32_t m, int32_t d, int32_t k);
 CT_API int ct_batch_free(ct_batch* b);
 
 /*
@@ -224,8 +234,8 @@ CT_API int ct_batch_free(ct_batch* b);
  * points[inducing_idx]); v_out [n x m] and p_out [n] device f32.  lengthscale is the
  * scalar the reference's builder takes; kernel_type CT_KERNEL_*.  ct_vfactor_create
  * synchronises `stream` and returns CT_ERR_ARG when k_mm is not positive definite
- * (numpy's LinAlgError).  Embeds on one factor share its scratch: calls whose GPU work
- * could overlap must use the same stream.
+ * (numpy's LinAlgError).  The factor is read-only after creation: embeds may run
+ * concurrently on different streams (each takes stream-ordered scratch of its own).
  */
 typedef struct ct_vfactor ct_vfactor;
 CT_API int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type, double variance,

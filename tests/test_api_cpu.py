@@ -54,3 +54,42 @@ def test_query_sharding_covers_every_query_once():
         parts = [bench.shard_queries(1001, world, r) for r in range(world)]
         allq = np.sort(np.concatenate(parts))
         assert np.array_equal(allq, np.arange(1001))
+
+
+def test_serving_stream_is_seeded_and_shaped():
+    from covertreex_gb300.synthetic import serving_stream
+
+    pre, s1 = serving_stream(500.0, 0.2, seed=6, preload=2)
+    _, s2 = serving_stream(500.0, 0.2, seed=6, preload=2)
+    assert [r.rid for r in s1] == [r.rid for r in s2]
+    assert all(a.arrival <= b.arrival for a, b in zip(s1, s1[1:]))
+    builds = [r for r in s1 if hasattr(r, "coords")]
+    queries = [r for r in s1 if hasattr(r, "points")]
+    assert len(pre) == 2 and len(queries) > len(builds)
+    for b in pre + builds:
+        assert 1024 <= b.coords.shape[0] <= 131072 and b.coords.shape[1] == 3 and b.inducing_count == 256
+        assert 0.5 <= b.lengthscale <= 2.0 and b.kernel_type == 1
+    known = {b.rid for b in pre + builds}
+    for q in queries:
+        assert 1 <= q.points.shape[0] <= 4096 and q.k in (30, 50, 60) and q.tree in known
+
+
+def test_batch_trees_shapes():
+    from covertreex_gb300.synthetic import batch_trees
+
+    trees = batch_trees()
+    assert len(trees) == 64
+    assert all(2048 <= t.n <= 65536 and t.d in (2, 3, 5) and t.m == 128 and t.k in (10, 30, 50) for t in trees)
+    assert {t.kernel_type for t in trees} == {0, 1} and {t.predecessor for t in trees} == {False, True}
+
+
+def test_serving_estimates_and_summary():
+    from covertreex_gb300.serving import RequestRecord, estimate_tree_bytes, latency_summary
+
+    assert estimate_tree_bytes(1000, 3, 256) < estimate_tree_bytes(2000, 3, 256) < estimate_tree_bytes(2000, 3, 512)
+    recs = [RequestRecord(rid=i, kind="query", arrival=0.001 * i, size=10, done=0.001 * i + 0.002, status="ok",
+                          form="dense") for i in range(100)]
+    recs.append(RequestRecord(rid=100, kind="query", arrival=0.0, size=5, status="evicted"))
+    s = latency_summary(recs)
+    assert s["count"] == 100 and s["dropped"] == 1
+    assert abs(s["p50_ms"] - 2.0) < 1e-6 and abs(s["p99_ms"] - 2.0) < 1e-6

@@ -113,3 +113,42 @@ def test_cover_tree_with_device_vmatrix(cuda_available):
     idx_gpu = t_gpu.knn(10, queries=np.arange(0, 3000, 7), predecessor_mode=True, form="dense")
     ref = O.brute_knn_f32(V, p, X, 1.0, np.ones(3, np.float32), 1, np.arange(0, 3000, 7), 10, predecessor=True)
     assert np.array_equal(np.asarray(idx_gpu), ref[0])
+
+
+def test_concurrent_embeds_on_one_factor(cuda_available):
+    """Two threads embed through one factor on their own streams, with batch sizes
+    that differ call to call: the factor is read-only, each call's scratch is its
+    own, and every result equals the single-threaded one."""
+    import threading
+
+    import torch
+
+    from covertreex_gb300.device import CudaVFactor
+
+    X = np.random.default_rng(21).standard_normal((4000, 3))
+    f = CudaVFactor(X[:256], kernel_type=1, variance=1.0, lengthscale=1.0)
+    sizes = [1, 37, 4096, 700, 9000, 5]
+    pts = [np.random.default_rng(100 + i).standard_normal((q, 3)) for i, q in enumerate(sizes)]
+    ref = [f.embed(p) for p in pts]
+    errors = []
+
+    def work(order):
+        st = torch.cuda.Stream()
+        try:
+            for _ in range(3):
+                for i in order:
+                    with torch.cuda.stream(st):
+                        v, p = f.embed_device(pts[i], stream=st)
+                        v, p = v.cpu().numpy(), p.cpu().numpy()
+                    if not (np.array_equal(v, ref[i][0]) and np.array_equal(p, ref[i][1])):
+                        errors.append(i)
+        except Exception as exc:  # surfaced below
+            errors.append(repr(exc))
+
+    ts = [threading.Thread(target=work, args=(o,)) for o in ([0, 2, 4, 1, 3, 5], [5, 3, 1, 4, 2, 0])]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    f.free()
+    assert not errors, errors

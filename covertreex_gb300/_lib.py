@@ -28,6 +28,7 @@ CT_FORM_DENSE = 0
 CT_FORM_TREE = 1
 CT_FORM_SCREENED = 2
 CT_BUILD_METRIC_ONLY = 1
+CT_BUILD_QUERY_SLAB = 2
 CT_NOALLOC_SCRATCH_BYTES = 64 << 20
 
 FORMS = {"dense": CT_FORM_DENSE, "tree": CT_FORM_TREE, "screened": CT_FORM_SCREENED}

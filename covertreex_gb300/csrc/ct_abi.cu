@@ -94,6 +94,7 @@ int ct_build_residual(const float* v, const float* p, const float* coords, int64
     if (!T) return fail(CT_ERR_NOMEM, "ct_build_residual: host allocation failed");
     T->n = n; T->m = m; T->d = d; T->var = variance; T->kernel_type = kernel_type;
     T->chunk = chunk > 0 ? chunk : 512; T->order_mode = order; T->seed = seed;
+    T->slab_rows = (flags & CT_BUILD_QUERY_SLAB) ? 4096 : 0;
 
     // inverse lengthscales exactly as ResidualMetric::new (src/metric.rs:93-101)
     float inv_ls[64];
@@ -308,12 +309,12 @@ int ct_vfactor_create(const double* z, int32_t m, int32_t d, int32_t kernel_type
     cudaError_t e = cudaMalloc((void**)&F->z, sizeof(double) * (size_t)m * d);
     if (e == cudaSuccess) e = cudaMalloc((void**)&F->L, sizeof(double) * mm);
     if (e == cudaSuccess) e = cudaMalloc((void**)&F->Li, sizeof(double) * mm);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&status, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(F->z, z, sizeof(double) * (size_t)m * d, cudaMemcpyDeviceToDevice, st);
     if (e == cudaSuccess) e = ct::vmatrix_factor(F->z, m, d, kernel_type, variance, lengthscale, F->L, F->Li, status, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (status) cudaFreeAsync(status, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (status) cudaFree(status);
     if (e != cudaSuccess) { int r = cuda_fail(e, "ct_vfactor_create"); ct_vfactor_free(F); return r; }
     if (hs) {
         ct_vfactor_free(F);

@@ -639,13 +639,22 @@ int ct_batch_autotune(ct_batch* B, int32_t reps, void* stream, int32_t* qt_out, 
     const int ipss[3] = {1, 4, 16};
     float best = 3.4e38f;
     int bq = 0, bc = 0, bi = 0;
+    bool primed = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     for (const Shape& s : shapes) {
         if (!shape_fits(B, s.qt, s.cps)) continue;
+        std::vector<std::vector<int>> seen;  // split patterns already timed for this shape
         for (int ips : ipss) {
-            int rc = run_shape(B, s.qt, s.cps, ips, false, st);  // warm-up (and first touch)
+            Plan P;
+            make_plan(B, s.qt, s.cps, ips, P);
+            std::vector<int> splits;
+            for (const Problem& pr : P.probs) splits.push_back(pr.split);
+            if (std::find(seen.begin(), seen.end(), splits) != seen.end()) continue;  // same launch
+            seen.push_back(splits);
+            int rc = CT_OK;
+            if (!primed) { rc = run_shape(B, s.qt, s.cps, ips, false, st); primed = true; }  // first-touch costs
             if (rc == CT_OK) cudaEventRecord(e0, st);
             for (int r = 0; r < reps && rc == CT_OK; ++r) rc = run_shape(B, s.qt, s.cps, ips, false, st);
             if (rc != CT_OK) {

@@ -1030,7 +1030,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, bytes ? bytes : 16); };
     A((void**)&S->hil_order, sizeof(int) * n);
-    A((void**)&S->hil_key, sizeof(unsigned long long) * n);
+    A((void**)&S->hil_key, sizeof(unsigned long long) * (n + T->slab_rows));
     A((void**)&S->ds_hi, sizeof(bf16) * S->rows_pad * m);
     A((void**)&S->ds_lo, sizeof(bf16) * S->rows_pad * m);
     A((void**)&S->b_id_ds, sizeof(int) * S->rows_pad);
@@ -1039,12 +1039,17 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->lvl_id, sizeof(int) * S->lvl_rows);
     A((void**)&S->lvl_key, sizeof(unsigned long long) * S->lvl_rows);
     A((void**)&S->lvl_meta, sizeof(long long) * 3 * S->levels.size());
-    A((void**)&S->vn, sizeof(float) * n);
-    A((void**)&S->isp, sizeof(float) * n);
-    A((void**)&S->xmax, sizeof(float) * n);
+    const long long rows_q = n + T->slab_rows;  // per-row scalars cover the query slab
+    A((void**)&S->vn, sizeof(float) * rows_q);
+    A((void**)&S->isp, sizeof(float) * rows_q);
+    A((void**)&S->xmax, sizeof(float) * rows_q);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->status, sizeof(int));
     A((void**)&S->bounds, sizeof(double) * 2 * 64);
+    if (e == cudaSuccess && T->slab_rows > 0) {
+        e = cudaEventCreateWithFlags(&S->slab_done, cudaEventDisableTiming);
+        S->slab_cap = T->slab_rows;
+    }
     if (e != cudaSuccess) return T->set_err(CT_ERR_NOMEM, "screen prep allocation: %s", cudaGetErrorString(e));
     e = ct::compute_order(T->coords_raw, n, T->d, 1, S->hil_order, st, S->hil_key, S->bounds);
     std::vector<int> order_h(n);
@@ -1425,7 +1430,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
 
 // Device bytes of the metric arrays, the cover tree and the screened operands.
 long long ct_tree::device_bytes() const {
-    const long long rows = n + (screen ? ((const State*)screen)->slab_cap : 0);
+    const long long rows = n + std::max<long long>(slab_rows, screen ? ((const State*)screen)->slab_cap : 0);
     long long b = (long long)n * m * 4 + n * (long long)d * 4 + n * 8 + 64 * 4;  // vperm, xs (dataset part), norms, p
     b += rows * (long long)m * 4 + rows * (long long)d * 8 + rows * 4;           // vnat, coords_raw + slab xs, slab p
     if (has_tree) b += n * (8 * 6 + 4 + 4) + (long long)n * (m + d + 2) * 4;
@@ -1485,13 +1490,12 @@ int ensure_slab(ct_tree* T, State* S, long long rows) {
 
 }  // namespace
 
-// Build the screened operands and a query slab of 4096 rows ahead of the first query.
+// Build the screened operands ahead of the first query (the query slab, if the tree
+// was built with CT_BUILD_QUERY_SLAB, is already allocated).
 int ct_tree::prepare_screened(cudaStream_t st) {
     if (m % KC != 0 || m > 1024) return set_err(CT_ERR_UNSUPPORTED, "screened form needs m %% 32 == 0 and m <= 1024 (got %d)", m);
     if (d > kMaxD) return set_err(CT_ERR_UNSUPPORTED, "screened form supports d <= %d (got %d)", kMaxD, d);
-    int rc = screen_prepare(this, st);
-    if (rc == CT_OK) rc = ensure_slab(this, (State*)screen, 4096);
-    return rc;
+    return screen_prepare(this, st);
 }
 
 // kNN of new points with the screened form: the points are written to the query

@@ -17,13 +17,14 @@ void dfree(T*& p) {
 }  // namespace
 
 int ct_tree::alloc_metric() {
+    const size_t rows = (size_t)(n + slab_rows);  // query-side arrays carry the slab
     cudaError_t e = dalloc(&vperm, (size_t)n * m);
-    if (e == cudaSuccess) e = dalloc(&xs, (size_t)n * d);
+    if (e == cudaSuccess) e = dalloc(&xs, rows * d);
     if (e == cudaSuccess) e = dalloc(&norms, (size_t)n);
-    if (e == cudaSuccess) e = dalloc(&p, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&p, rows);
     if (e == cudaSuccess) e = dalloc(&inv_ls, (size_t)64);
-    if (e == cudaSuccess) e = dalloc(&vnat, (size_t)n * m);
-    if (e == cudaSuccess) e = dalloc(&coords_raw, (size_t)n * d);
+    if (e == cudaSuccess) e = dalloc(&vnat, rows * m);
+    if (e == cudaSuccess) e = dalloc(&coords_raw, rows * d);
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "device allocation of %lld x %d metric rows failed: %s",
                                          (long long)n, m, cudaGetErrorString(e));
     return CT_OK;

@@ -14,6 +14,7 @@ struct ct_tree {
     float var = 1.f;
     int kernel_type = 0;
     int chunk = 512, order_mode = CT_ORDER_HILBERT;
+    long long slab_rows = 0;  // rows reserved past n in vnat / xs / coords_raw / p for new points
     uint64_t seed = 0;
 
     // metric data (dataset order), see ct_setup.cu

@@ -45,7 +45,7 @@ class CudaResidualIndex:
 
     def __init__(self, v_matrix, p_diag, coords, *, variance: float = 1.0, lengthscale=1.0, kernel_type: int = 0,
                  chunk_size: int = 512, order: str = "hilbert", seed: int = 0, build_tree: bool = True,
-                 device=None, stream=None):
+                 query_slab: bool = False, device=None, stream=None):
         torch = _torch()
         self.device = torch.device(device if device is not None else "cuda")
         L = _lib.load()
@@ -65,6 +65,8 @@ class CudaResidualIndex:
         self.has_tree = bool(build_tree)
         order_code = _lib.CT_ORDER_NATURAL if str(order).lower() == "natural" else _lib.CT_ORDER_HILBERT
         flags = 0 if build_tree else _lib.CT_BUILD_METRIC_ONLY
+        if query_slab:
+            flags |= _lib.CT_BUILD_QUERY_SLAB
         h = ctypes.c_void_p()
         ls_c = (ctypes.c_float * ls.size)(*ls.tolist())
         with torch.cuda.device(self.device):

@@ -96,8 +96,9 @@ class ResidentTree:
 class _Step:
     slot: int
     event: object
-    items: list = field(default_factory=list)   # (record, idx_host, dist_host)
+    items: list = field(default_factory=list)   # (record, idx_host, dist_host, _, _)
     trees: list = field(default_factory=list)
+    buffers: tuple = ()
 
 
 def estimate_tree_bytes(n: int, d: int, m: int) -> int:
@@ -114,7 +115,7 @@ def estimate_tree_bytes(n: int, d: int, m: int) -> int:
 
 class ServingEngine:
     def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 2, max_step_points: int = 16384,
-                 dense_pair_limit: float = 3.0e10, device=None, reserve=(256, 3, 64)):
+                 dense_pair_limit: float = 1.0e11, device=None, reserve=(256, 3, 64)):
         import torch
 
         from .device import CudaBatch
@@ -164,7 +165,8 @@ class ServingEngine:
                             lengthscale=req.lengthscale, device=self.device, stream=st)
             V, p = f.embed_device(xd, stream=st)
             index = CudaResidualIndex(V, p, xd, variance=req.variance, lengthscale=req.lengthscale,
-                                      kernel_type=req.kernel_type, build_tree=False, device=self.device, stream=st)
+                                      kernel_type=req.kernel_type, build_tree=False, query_slab=True,
+                                      device=self.device, stream=st)
             if index.m % 32 == 0 and index.d <= 8:
                 index.prepare_screened(stream=st)
             del V, p, xd
@@ -249,22 +251,28 @@ class ServingEngine:
                 tree.last_used = time.perf_counter()
                 step.trees.append(tree)
                 groups.setdefault(tree.rid, []).append((rec, req, tree))
-            outs = []
+            # one device and one pinned host buffer for every result row of the step
+            total = sum(int(req.points.shape[0]) * int(req.k) for _, req, _ in items)
+            d_idx = torch.empty(total, dtype=torch.int64, device=self.device)
+            d_dist = torch.empty(total, dtype=torch.float32, device=self.device)
+            h_idx = torch.empty(total, dtype=torch.int64, pin_memory=True)
+            h_dist = torch.empty(total, dtype=torch.float32, pin_memory=True)
+            off = 0
             for members in groups.values():
                 tree = members[0][2]
                 views = self._embed_group(tree, [m[1] for m in members], st)
                 for (rec, req, _), (x, qv, qp) in zip(members, views):
                     rec.form = "dense"
-                    idx, dist = b.add_points(tree.index, qv, qp, x, req.k)
-                    outs.append((rec, idx, dist))
+                    q, k = int(req.points.shape[0]), int(req.k)
+                    sl = slice(off, off + q * k)
+                    b.add_points(tree.index, qv, qp, x, k, out=(d_idx[sl].view(q, k), d_dist[sl].view(q, k)))
+                    step.items.append((rec, h_idx[sl].view(q, k), h_dist[sl].view(q, k), None, None))
+                    off += q * k
             b.run(use_graph=True, stream=st)
             self.launches += 1
-            for rec, idx, dist in outs:
-                hi = torch.empty(idx.shape, dtype=idx.dtype, pin_memory=True)
-                hd = torch.empty(dist.shape, dtype=dist.dtype, pin_memory=True)
-                hi.copy_(idx, non_blocking=True)
-                hd.copy_(dist, non_blocking=True)
-                step.items.append((rec, hi, hd, idx, dist))
+            h_idx.copy_(d_idx, non_blocking=True)
+            h_dist.copy_(d_dist, non_blocking=True)
+            step.buffers = (d_idx, d_dist, h_idx, h_dist)
             step.event.record(st)
         return step
 
@@ -272,7 +280,7 @@ class ServingEngine:
         for rec, hi, hd, _, _ in step.items:
             rec.done = now
             rec.status = "ok"
-            rec.result = (hi.numpy(), hd.numpy())
+            rec.result = (hi.numpy().copy(), hd.numpy().copy())
         for t in step.trees:
             t.inflight -= 1
         step.items = []

@@ -121,12 +121,14 @@ def tree_coords(spec: TreeSpec) -> np.ndarray:
 # ---------------------------------------------------------------------------
 def serving_stream(rate: float, duration: float, *, seed: int = 6, preload: int = 8, build_frac: float = 0.1,
                    n_min: int = 1024, n_max: int = 131072, m: int = 256, q_max: int = 4096,
-                   ks=(30, 50, 60), working_set: int = 32):
+                   ks=(30, 50, 60), working_set: int = 32, lag: float = 0.5):
     """Returns (preload_builds, stream).  Arrivals are Poisson at `rate` requests/s
     over `duration` seconds.  Builds (fraction `build_frac`): N log-uniform in
     [1k, 128k], D = 3, N(0,1) coordinates, Matern 5/2 with lengthscale U[0.5, 2],
     m = 256.  Queries: 1..4096 new N(0,1) points (log-uniform count), k drawn from
-    {30, 50, 60}, against a tree drawn from the most recent `working_set` builds."""
+    {30, 50, 60}, against a tree drawn from the most recent `working_set` trees among
+    the preloaded ones and the builds that arrived at least `lag` seconds earlier (a
+    client queries a tree once it has had time to be built)."""
     from .serving import BuildRequest, QueryRequest
 
     r = np.random.default_rng(seed)
@@ -144,7 +146,7 @@ def serving_stream(rate: float, duration: float, *, seed: int = 6, preload: int 
         return b
 
     pre = [make_build(0.0) for _ in range(preload)]
-    recent = [b.rid for b in pre]
+    ready = [(-1.0, b.rid) for b in pre]   # (arrival, rid) of trees a query may target
     stream = []
     t = 0.0
     while True:
@@ -154,11 +156,12 @@ def serving_stream(rate: float, duration: float, *, seed: int = 6, preload: int 
         if r.random() < build_frac:
             b = make_build(t)
             stream.append(b)
-            recent = (recent + [b.rid])[-working_set:]
+            ready.append((t, b.rid))
         else:
             q = int(np.clip(np.floor(np.exp(r.uniform(0.0, np.log(q_max)))), 1, q_max))
             pts = r.standard_normal((q, 3)).astype(np.float32)
-            stream.append(QueryRequest(rid=rid, arrival=t, tree=int(r.choice(recent)), points=pts,
+            pool = [rid_ for (a, rid_) in ready if a <= t - lag][-working_set:]
+            stream.append(QueryRequest(rid=rid, arrival=t, tree=int(r.choice(pool)), points=pts,
                                        k=int(r.choice(ks))))
             rid += 1
     return pre, stream

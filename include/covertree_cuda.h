@@ -64,6 +64,7 @@ extern "C" {
 
 /* build flags */
 #define CT_BUILD_METRIC_ONLY 1   /* skip the cover-tree build (dense / screened forms only) */
+#define CT_BUILD_QUERY_SLAB 2    /* reserve 4096 rows for new points of the screened form (serving) */
 
 typedef struct ct_tree ct_tree;
 

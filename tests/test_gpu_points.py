@@ -35,7 +35,9 @@ def test_new_points_dense_and_screened(cuda_available, case):
     n, d, m, kt, ls, k, nq = case
     X, V, p, Xq, qv, qp = _case(n, d, m, kt, ls, nq, seed=n + d)
     lsv = np.full(d, ls, np.float32)
-    index = CudaResidualIndex(V, p, X, variance=1.0, lengthscale=ls, kernel_type=kt, build_tree=False)
+    # the largest case starts from a reserved 4096-row query slab and outgrows it
+    index = CudaResidualIndex(V, p, X, variance=1.0, lengthscale=ls, kernel_type=kt, build_tree=False,
+                              query_slab=nq > 4096)
     # dense: bit-exact against the f32 oracle of new points
     di, dd = index.knn_points_device(qv, qp, Xq, k, form="dense")
     ref = O.brute_knn_points_f32(V, p, X, 1.0, lsv, kt, qv, qp, Xq, k)

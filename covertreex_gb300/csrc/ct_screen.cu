@@ -151,7 +151,8 @@ __device__ __forceinline__ void heap_push(float* h, int n, float x) {
 // bit 2 of `which`: a kept job whose candidate tile already fed the heap during warm-up
 __device__ __forceinline__ bool jb_warm_seen(const Job& jb) { return (jb.which & 4) != 0; }
 
-template <int MODE>
+// DP: coordinates read per candidate (4 when D <= 4, else 8).
+template <int MODE, int DP>
 __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -354,17 +355,30 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     continue;
                 }
                 if (qid < 0) continue;
+                // Phase 1, no stores: certified bounds of the group's 8 pairs, as
+                //   blo = (R - e) * isc (heap test)  and  bhi = (R + e) * isc (survivor test),
+                // +inf for the query itself, -inf for padding and predecessor-violating pairs.
+                // Free of stores, the pairs' loads and arithmetic overlap.
+                float blo[8], bhi[8];
+                int bid[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     const float4* r4 = (const float4*)(rb + (col0 + i) * REC);
                     const float4 meta = r4[2];
                     const int cid = __float_as_int(meta.w);
-                    if (cid < 0 || (P.predecessor && cid >= qid)) continue;
-                    const float4 xa = r4[0], xb = r4[1];
-                    const float xc[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-                    float d2 = 0.f;
-#pragma unroll
-                    for (int c = 0; c < kMaxD; ++c) { const float t = xq[c] - xc[c]; d2 = fmaf(t, t, d2); }
+                    const float4 xa = r4[0];
+                    float d2 = 0.f, t;
+                    t = xq[0] - xa.x; d2 = fmaf(t, t, d2);
+                    t = xq[1] - xa.y; d2 = fmaf(t, t, d2);
+                    t = xq[2] - xa.z; d2 = fmaf(t, t, d2);
+                    t = xq[3] - xa.w; d2 = fmaf(t, t, d2);
+                    if (DP > 4) {
+                        const float4 xb = r4[1];
+                        t = xq[4] - xb.x; d2 = fmaf(t, t, d2);
+                        t = xq[5] - xb.y; d2 = fmaf(t, t, d2);
+                        t = xq[6] - xb.z; d2 = fmaf(t, t, d2);
+                        t = xq[7] - xb.w; d2 = fmaf(t, t, d2);
+                    }
                     // Certified error of the kernel value.  d2 error: (D+2) 2^-24 d2 from the
                     // sum plus 2^-22 sum|dx| (|x_q| + |x_c|) from the scaled coordinates, with
                     // sum|dx| <= sqrt(D d2) <= (D d2 + 1) / 2.
@@ -382,15 +396,24 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     }
                     const float R = fabsf(kv - v[i]);
                     const float e = fmaf(vnq, meta.x, ek) + fmaf(R, 1.2e-7f, 1e-30f);
-                    const bool self = cid == qid;
-                    if (keep_job && (self || (R + e) * meta.y >= thr_keep)) {
-                        if (cnt < HALF_CAP) P.surv[((size_t)slot * 2 + half) * HALF_CAP + cnt] = cid;
+                    const bool valid = cid >= 0 && !(P.predecessor && cid >= qid);
+                    const float inf = __int_as_float(0x7f800000);
+                    blo[i] = !valid ? -inf : (cid == qid ? inf : (R - e) * meta.y);
+                    bhi[i] = !valid ? -inf : (cid == qid ? inf : (R + e) * meta.y);
+                    bid[i] = cid;
+                }
+                // Phase 2: survivors and heap against the current thresholds.  Phase 1's
+                // values do not depend on the thresholds, so this keeps and heaps exactly
+                // the pairs that pair-by-pair processing would.
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    if (keep_job && bhi[i] >= thr_keep) {
+                        if (cnt < HALF_CAP) P.surv[((size_t)slot * 2 + half) * HALF_CAP + cnt] = bid[i];
                         ++cnt;
                     }
-                    if (feed_heap && (self || (R - e) * meta.y > thr_heap)) {
-                        // exact certified upper bound of d^2 for this pair
-                        const float du2 = self ? 0.f
-                                               : 1.f - fminf(fmaxf(R - e, 0.f) * (isq * meta.y) * (1.f - 1e-6f), 1.f);
+                    if (feed_heap && blo[i] > thr_heap) {
+                        // exact certified upper bound of d^2 for this pair (0 for the query itself)
+                        const float du2 = 1.f - fminf(fmaxf(blo[i], 0.f) * isq * (1.f - 1e-6f), 1.f);
                         bool changed = false;
                         if (hn < P.k) {
                             heap_push(heap, hn, du2);
@@ -980,13 +1003,17 @@ static cudaError_t launch_sweep(const MMAParams& P, int mode, int ncta, cudaStre
     const size_t smem = smem_layout(P.k, P.nstages).total;
     cudaError_t e;
     if (mode == MODE_DEBUG) {
-        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_DEBUG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_DEBUG, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        screen_sweep_kernel<MODE_DEBUG><<<ncta, kThreads, smem, st>>>(P);
+        screen_sweep_kernel<MODE_DEBUG, 8><<<ncta, kThreads, smem, st>>>(P);
+    } else if (P.d <= 4) {
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        screen_sweep_kernel<MODE_SWEEP, 4><<<ncta, kThreads, smem, st>>>(P);
     } else {
-        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        screen_sweep_kernel<MODE_SWEEP><<<ncta, kThreads, smem, st>>>(P);
+        screen_sweep_kernel<MODE_SWEEP, 8><<<ncta, kThreads, smem, st>>>(P);
     }
     return cudaGetLastError();
 }

@@ -531,6 +531,9 @@ struct RescoreParams {
     int k;
     long long* out_idx; float* out_dist;
     long long* evals;
+    // visiting order of the survivor pass: query slots in the sweep's (Hilbert) order,
+    // each followed by its candidate parts, so neighbouring warps gather overlapping rows
+    const int* order; int parts;
 };
 
 // Compensated FP32 dot product pieces (TwoProd via FMA, TwoSum).  The warp
@@ -545,12 +548,6 @@ __device__ __forceinline__ void two_sum_acc(float& s, float& comp, float a, floa
     const float se = (s - (ts - z)) + (pr - z);
     s = ts;
     comp += se + pe;
-}
-
-__device__ __forceinline__ double warp_sum_double(double v) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    return v;
 }
 
 // Load the query slice: lane l holds elements [l*m/32, (l+1)*m/32).
@@ -601,8 +598,23 @@ __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, co
             }
         }
     }
+    // Warp reduction in double-float: a butterfly of TwoSum on the (sum, compensation)
+    // pairs, so every lane ends with the same value; one conversion to FP64 per dot.
 #pragma unroll
-    for (int c = 0; c < NC; ++c) out[c] = warp_sum_double((double)s[c] + (double)comp[c]);
+    for (int c = 0; c < NC; ++c) {
+        float hi = s[c], lo = comp[c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
+            const float t = hi + oh;
+            const float z = t - hi;
+            const float err = (hi - (t - z)) + (oh - z);
+            hi = t;
+            lo = (lo + ol) + err;
+        }
+        out[c] = (double)hi + (double)lo;
+    }
 }
 
 // FP64 kernel value, normalisation and square root for one pair (one lane).
@@ -643,7 +655,8 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
     long long w = (long long)blockIdx.x * wpb + warp;
     long long nwork = use_full ? P.nfull : P.nslots;
     if (w >= nwork) return;
-    const int slot = use_full ? P.full_slots[w] : (int)w;
+    const int slot = use_full ? P.full_slots[w]
+                              : (P.order ? P.order[w / P.parts] * P.parts + (int)(w % P.parts) : (int)w);
     const int c0 = use_full ? 0 : P.surv_cnt[2 * slot];
     const int c1 = use_full ? 0 : P.surv_cnt[2 * slot + 1];
     if (!use_full && (c0 > HALF_CAP || c1 > HALF_CAP)) return;  // handled by the exhaustive pass
@@ -721,7 +734,9 @@ __device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& 
     __syncwarp();
 }
 
-__global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, int nitems,
+// Warp w scores item perm[w]: items are visited chunk-major, so the warps in flight
+// stream the same candidate rows; results land at the item's slot-major index.
+__global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, const int* perm, int nitems,
                                      unsigned long long* partial) {
     extern __shared__ unsigned long long ckeys_all[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -729,7 +744,8 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, in
     unsigned long long* keys = ckeys_all + (size_t)warp * RBUF;
     const long long w = (long long)blockIdx.x * wpb + warp;
     if (w >= nitems) return;
-    const ChunkItem it = items[w];
+    const int wi = perm[w];
+    const ChunkItem it = items[wi];
     const int q = P.slot_id[it.slot];
     const int k = P.k;
     float vql[32];
@@ -758,7 +774,7 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, in
         warp_topk_append(keys, fill, k, lane < nb, pack_key(dist, cid));
     }
     warp_bitonic_sort(keys);
-    for (int j = lane; j < k; j += 32) partial[(size_t)w * k + j] = keys[j];
+    for (int j = lane; j < k; j += 32) partial[(size_t)wi * k + j] = keys[j];
     if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)(b1 - b0));
 }
 
@@ -1348,6 +1364,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list;
     R.nfull = 0;
     R.k = k; R.evals = evals_d;
+    R.order = val_lvl; R.parts = parts;
     R.out_idx = parts > 1 ? part_idx : (long long*)out_idx;
     R.out_dist = parts > 1 ? part_dist : out_dist;
     const int rwpb = 8;
@@ -1365,6 +1382,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     ChunkItem* items_d = nullptr;
     int* item_begin_d = nullptr;
+    int* perm_d = nullptr;
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess && nfull > 0) {
         // split every overflowed slot's exhaustive range into chunks
@@ -1382,17 +1400,22 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         }
         ibeg[nfull] = (int)items.size();
         const int nitems = (int)items.size();
+        std::vector<int> perm(nitems);
+        for (int i = 0; i < nitems; ++i) perm[i] = i;
+        std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return items[a].chunk < items[b].chunk; });
         A((void**)&items_d, sizeof(ChunkItem) * (nitems + 1));
+        A((void**)&perm_d, sizeof(int) * (nitems + 1));
         A((void**)&item_begin_d, sizeof(int) * (nfull + 1));
         A((void**)&partial, sizeof(unsigned long long) * ((size_t)nitems * k + 1));
         if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(items_d, items.data(), sizeof(ChunkItem) * nitems, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(perm_d, perm.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, st);
         R.nfull = nfull;
         if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(merge_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (e == cudaSuccess && nitems > 0) {
-            rescore_chunk_kernel<<<(unsigned)((nitems + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, items_d, nitems, partial);
+            rescore_chunk_kernel<<<(unsigned)((nitems + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, items_d, perm_d, nitems, partial);
             merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, item_begin_d, partial);
             e = cudaGetLastError();
             launches += 2;
@@ -1436,6 +1459,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (part_idx) cudaFreeAsync(part_idx, st);
     if (part_dist) cudaFreeAsync(part_dist, st);
     if (items_d) cudaFreeAsync(items_d, st);
+    if (perm_d) cudaFreeAsync(perm_d, st);
     if (item_begin_d) cudaFreeAsync(item_begin_d, st);
     if (partial) cudaFreeAsync(partial, st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form: %s", cudaGetErrorString(e));

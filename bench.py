@@ -48,6 +48,9 @@ def parse_args():
     ap.add_argument("--cpu-sample", type=int, default=2048, help="queries per CPU baseline sample")
     ap.add_argument("--n", type=int, default=None, help="override N of the workload (profiling on a smaller case)")
     ap.add_argument("--no-batching", action="store_true", help="skip the 64-tree batching-form measurement")
+    ap.add_argument("--batch-trees", type=int, default=64, help="trees of the batching form (fewer for profiling)")
+    ap.add_argument("--no-headline", action="store_true",
+                    help="skip the precision-form workload (profiling the batching form alone)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
     ap.add_argument("--serving-rates", default="100,500,1000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--serving-seconds", type=float, default=2.0, help="arrival window per serving rate")
@@ -199,7 +202,7 @@ def fp32_core_peak(sm_mhz):
     return sms * 128 * mhz * 1e6 / 1e12
 
 
-def bench_batching(dev, steps: int = 3, warmup: int = 1):
+def bench_batching(dev, steps: int = 3, warmup: int = 1, count: int = 64):
     """64 independent trees (N log-uniform [2048, 65536], D in {2,3,5}, Matern/RBF
     alternating, m = 128, k in {10,30,50}, predecessor alternating), every point of
     every tree queried: one persistent launch per step (CUDA-graph replay, autotuned
@@ -210,7 +213,7 @@ def bench_batching(dev, steps: int = 3, warmup: int = 1):
     from covertreex_gb300.device import CudaBatch, CudaResidualIndex, CudaVFactor
     from covertreex_gb300.residual import inducing_indices
 
-    specs = synthetic.batch_trees()
+    specs = synthetic.batch_trees(count=count)
     trees = []
     t0 = time.perf_counter()
     for sp in specs:
@@ -268,7 +271,7 @@ def bench_batching(dev, steps: int = 3, warmup: int = 1):
         index.free()
     b.free()
     return {
-        "workload": "64 trees: N log-uniform [2048, 65536], D in {2,3,5}, Matern 5/2 / RBF alternating, "
+        "workload": f"{len(specs)} trees: N log-uniform [2048, 65536], D in {{2,3,5}}, Matern 5/2 / RBF alternating, "
                     "lengthscale U[0.5,2], m=128, k in {10,30,50}, predecessor alternating; all N ids queried",
         "trees": len(specs), "queries": nq, "pairs": pairs,
         "ms_per_step": step_ms, "queries_per_s": nq / (step_ms / 1e3),
@@ -354,6 +357,15 @@ def main():
 
     _build.build_library()
     L = _lib.load()
+    if args.no_headline:
+        # profiling aid: the batching / serving forms alone (not the bench line)
+        dev = torch.device("cuda", local)
+        out = {"batching": None if args.no_batching else bench_batching(dev, count=args.batch_trees),
+               "serving": None if args.no_serving else bench_serving(
+                   dev, [float(x) for x in args.serving_rates.split(",") if x], args.serving_seconds)}
+        if rank == 0:
+            print(json.dumps(out))
+        return
     wl = synthetic.make(args.workload, n=args.n)
     dev = torch.device("cuda", local)
     index = CudaResidualIndex(wl.v, wl.p, wl.coords, variance=wl.variance, lengthscale=[wl.lengthscale] * wl.d,
@@ -458,9 +470,14 @@ def main():
     alg_flops = 2.0 * wl.m * pairs_main             # per-unit figure 2m flops per screened pair
     issued_flops = 3.0 * alg_flops                  # hi.hi + hi.lo + lo.hi
     achieved = alg_flops / (screen_ms / 1e3) / 1e12
+    # DRAM bytes per screened pair of the sweep, from the ncu capture at N=65536 of the
+    # same workload (profiles/screen_sweep_precision_workload.md), scaled to this launch
+    sweep_dram_bytes_per_pair = 6.94
     roofline = {
-        "bound": "tensor", "kernel": "screen_mma_kernel (main sweep)", "achieved": achieved,
-        "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus, "traffic": None,
+        "bound": "tensor", "kernel": "screen_sweep_kernel (main sweep)", "achieved": achieved,
+        "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
+        "traffic": sweep_dram_bytes_per_pair * pairs_main,
+        "traffic_note": "bytes per launch: 6.94 B per screened pair (ncu, N=65536) x pairs of this launch",
         "peak_kind": f"bf16_tflops_sustained ({peak_kind})",
         "tensor_issued_tflops": issued_flops / (screen_ms / 1e3) / 1e12,
         "kernel_ms": screen_ms, "pairs_per_launch": pairs_main,
@@ -487,7 +504,7 @@ def main():
     serving = None
     if rank == 0 and world == 1 and not args.no_batching:
         try:
-            batching = bench_batching(dev)
+            batching = bench_batching(dev, count=args.batch_trees)
         except Exception as exc:
             batching = {"unavailable": repr(exc)}
     if rank == 0 and world == 1 and not args.no_serving:

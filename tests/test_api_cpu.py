@@ -93,3 +93,24 @@ def test_serving_estimates_and_summary():
     s = latency_summary(recs)
     assert s["count"] == 100 and s["dropped"] == 1
     assert abs(s["p50_ms"] - 2.0) < 1e-6 and abs(s["p99_ms"] - 2.0) < 1e-6
+
+
+def test_runtime_api_host_checks():
+    import pytest as _pytest
+
+    from covertreex_gb300 import CoverTree, Residual, Runtime, api
+
+    rt = Runtime(backend="numpy", precision="float32", metric="residual_correlation", enable_rust=True,
+                 engine="rust-natural", residual_use_static_euclidean_tree=True, residual=Residual(radius_floor=1e-3))
+    assert rt.is_residual and rt.with_updates(metric="euclidean").is_residual is False
+    with _pytest.raises(RuntimeError):
+        CoverTree(rt).knn(np.array([[0]]), k=1)       # not fitted
+    with _pytest.raises(ValueError):
+        CoverTree(rt).fit(np.zeros((0, 2)))           # no points
+    with _pytest.raises(ValueError):
+        CoverTree(Runtime(engine="no-such-engine")).fit(np.zeros((4, 2), np.float32))
+    api.reset_residual_correlation()
+    with _pytest.raises(RuntimeError):
+        api.get_residual_backend()
+    with _pytest.raises(ValueError):
+        api.configure_residual_correlation(None)

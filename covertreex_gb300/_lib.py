@@ -52,6 +52,7 @@ EXPORTED_SYMBOLS = (
     "ct_vfactor_free",
     "ct_knn_residual_points",
     "ct_prepare_screened",
+    "ct_tree_inputs",
     "ct_tree_device_bytes",
     "ct_batch_create",
     "ct_batch_clear",
@@ -146,6 +147,8 @@ def load(build_if_missing: bool = True):
         L.ct_vfactor_free.restype = ctypes.c_int
         L.ct_vfactor_free.argtypes = [vp]
         ip32 = ctypes.POINTER(i32)
+        L.ct_tree_inputs.restype = ctypes.c_int
+        L.ct_tree_inputs.argtypes = [vp, vp, vp, vp, vp]
         L.ct_prepare_screened.restype = ctypes.c_int
         L.ct_prepare_screened.argtypes = [vp, vp]
         L.ct_tree_device_bytes.restype = ctypes.c_int

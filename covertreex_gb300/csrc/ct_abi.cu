@@ -230,6 +230,16 @@ int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* c
     return rc == CT_OK ? CT_OK : fail(rc, "ct_knn_residual_dense_noalloc: %s", msg);
 }
 
+int ct_tree_inputs(const ct_tree* T, float* v, float* p, float* coords, void* stream) {
+    if (!T) return fail(CT_ERR_ARG, "ct_tree_inputs: tree is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)T->n;
+    if (v) CT_CUDA(cudaMemcpyAsync(v, T->vnat, n * T->m * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy v");
+    if (p) CT_CUDA(cudaMemcpyAsync(p, T->p, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy p");
+    if (coords) CT_CUDA(cudaMemcpyAsync(coords, T->coords_raw, n * T->d * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy coords");
+    return CT_OK;
+}
+
 int ct_prepare_screened(ct_tree* T, void* stream) {
     if (!T) return fail(CT_ERR_ARG, "ct_prepare_screened: tree is NULL");
     int rc = T->prepare_screened((cudaStream_t)stream);

@@ -77,6 +77,9 @@ class CudaResidualIndex:
         _lib.check(rc)
         self._h = h
         self.last_stats: dict = {}
+        self.last_form: str = ""
+        self.build_params = {"chunk_size": int(chunk_size), "order": str(order), "seed": int(seed),
+                             "build_tree": bool(build_tree), "query_slab": bool(query_slab)}
 
     # ------------------------------------------------------------------
     def knn_device(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense", stream=None,
@@ -101,7 +104,46 @@ class CudaResidualIndex:
                                          _stream_ptr(stream))
         _lib.check(rc)
         self.last_stats = st.as_dict()
+        self.last_form = form
         return idx, dist
+
+    # ------------------------------------------------------------------ telemetry
+    def last_query_telemetry(self):
+        """The last query's counters in the reference's ResidualQueryTelemetry shape
+        (src/telemetry.rs:1-19, returned by CoverTreeWrapper.last_query_telemetry,
+        src/lib.rs:357-363), with the GPU forms' own counters under "gpu"."""
+        from .telemetry import query_telemetry
+
+        return query_telemetry(self.last_stats, self.last_form) if self.last_stats else None
+
+    def clear_last_query_telemetry(self):
+        self.last_stats = {}
+        self.last_form = ""
+
+    # ------------------------------------------------------------------ persistence
+    def save(self, path) -> None:
+        """Write the index to a flat binary file: a JSON header line, then V [n, m],
+        p [n] and the raw coordinates [n, d] as little-endian f32.  ``load`` rebuilds
+        the device layouts and the cover tree from them with the same parameters, so
+        the loaded index answers every query exactly as this one."""
+        from .persist import save_index
+
+        save_index(self, path)
+
+    @classmethod
+    def load(cls, path, device=None, stream=None) -> "CudaResidualIndex":
+        from .persist import load_index
+
+        return load_index(path, device=device, stream=stream)
+
+    def inputs_device(self, stream=None):
+        """Device copies of (V natural [n, m], p [n], raw coordinates [n, d])."""
+        torch = _torch()
+        v = torch.empty((self.n, self.m), dtype=torch.float32, device=self.device)
+        p = torch.empty((self.n,), dtype=torch.float32, device=self.device)
+        c = torch.empty((self.n, self.d), dtype=torch.float32, device=self.device)
+        _lib.check(_lib.load().ct_tree_inputs(self._h, v.data_ptr(), p.data_ptr(), c.data_ptr(), _stream_ptr(stream)))
+        return v, p, c
 
     def knn(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense"):
         """Host-in / host-out kNN (numpy int64 [Q,k], float32 [Q,k])."""

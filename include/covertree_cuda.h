@@ -167,6 +167,11 @@ CT_API int ct_prepare_screened(ct_tree* tree, void* stream);
 /* Device memory held by a tree handle, in bytes (host output). */
 CT_API int ct_tree_device_bytes(const ct_tree* tree, int64_t* bytes);
 
+/* Copy the tree's inputs (V [n x m] natural order, p [n], raw coords [n x d]; dataset
+ * order; device f32; any may be NULL), e.g. to persist the tree.  No counterpart in
+ * the reference, which has no tree persistence. */
+CT_API int ct_tree_inputs(const ct_tree* tree, float* v, float* p, float* coords, void* stream);
+
 /* n, m, d of a tree (host outputs; any may be NULL). */
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);
 

@@ -114,3 +114,26 @@ def test_runtime_api_host_checks():
         api.get_residual_backend()
     with _pytest.raises(ValueError):
         api.configure_residual_correlation(None)
+
+
+def test_telemetry_formats(tmp_path):
+    import json as _json
+
+    from covertreex_gb300.telemetry import (BENCHMARK_BATCH_REQUIRED, BENCHMARK_BATCH_SCHEMA_ID,
+                                            BatchTelemetryWriter, query_telemetry)
+
+    # the field names of ResidualQueryTelemetry (src/telemetry.rs)
+    fields = ["frontier_levels", "frontier_expanded", "yields", "caps_applied", "prunes_lower_bound",
+              "prunes_lower_bound_chunks", "prunes_cap", "masked_dedup", "distance_evals", "budget_escalations",
+              "budget_early_terminate", "level_cache_hits", "level_cache_misses", "block_sizes",
+              "predecessor_filtered", "subtrees_pruned"]
+    t = query_telemetry({"distance_evals": 42, "pairs_screened": 7, "device_ms": 1.5}, "screened")
+    assert all(f in t for f in fields) and t["distance_evals"] == 42 and t["gpu"]["pairs_screened"] == 7
+    w = BatchTelemetryWriter(tmp_path / "t.jsonl", runtime={"engine": "cuda", "metric": "residual_correlation"})
+    w.record(batch_index=0, batch_size=512, measurements={"build_seconds": 0.01}, metadata={"n": 4096})
+    w.record(batch_index=1, batch_size=100, measurements={"queries_per_s": 1e6})
+    rows = [_json.loads(x) for x in (tmp_path / "t.jsonl").read_text().splitlines()]
+    assert [r["batch_event_index"] for r in rows] == [0, 1]
+    for r in rows:
+        assert all(k in r for k in BENCHMARK_BATCH_REQUIRED) and r["schema_id"] == BENCHMARK_BATCH_SCHEMA_ID
+    assert rows[0]["build_seconds"] == 0.01 and rows[1]["queries_per_s"] == 1e6

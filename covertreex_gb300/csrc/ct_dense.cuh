@@ -42,8 +42,10 @@ __host__ __device__ inline Smem layout(int qt, int m, int d, int k) {
     const int m16 = m / 16;
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 15) & ~size_t(15); return o; };
-    L.a = take(sizeof(float) * qt * (m + 1));
-    L.b = take(sizeof(float) * 2 * kCT * (m16 + 1));
+    // row strides: m + 4 / m16 + 4 floats (16-byte rows for the vector path); the
+    // scalar path uses m + 1 / m16 + 1 inside the same space
+    L.a = take(sizeof(float) * qt * (m + 4));
+    L.b = take(sizeof(float) * 2 * kCT * (m16 + 4));
     L.ds = take(sizeof(float) * qt * (kCT + 1));
     L.ld = take(sizeof(float) * qt * k);
     L.li = take(sizeof(int) * qt * k);
@@ -60,6 +62,10 @@ __host__ __device__ inline Smem layout(int qt, int m, int d, int k) {
     return L;
 }
 
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc) {
+    unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gsrc));
+}
 __device__ __forceinline__ void cp_async4(void* smem_dst, const void* gsrc) {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc));
@@ -134,8 +140,11 @@ struct Tile {
     long long out_stride;
 };
 
-template <int QT>
-__device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw) {
+// VEC = 4: shared-memory rows padded to 16 bytes, operands moved and read 4 floats at
+// a time (m a multiple of 64); VEC = 1: scalar (any m multiple of 16).  Both add the
+// products in the same order, so both give the same bits.
+template <int QT, int VEC>
+__device__ __forceinline__ void run_tile_v(const Tile& P, unsigned char* smem_raw) {
     const Smem S = layout(QT, P.m, P.d, P.k);
     float* As = (float*)(smem_raw + S.a);
     float* Bs = (float*)(smem_raw + S.b);
@@ -158,7 +167,7 @@ __device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw)
     const int lane = tid & 31, warp = tid >> 5;
     const int tq = tid >> 4, tc = tid & 15;
     const int m = P.m, m16 = m / 16, d = P.d, k = P.k;
-    const int AST = m + 1, BST = m16 + 1;
+    const int AST = VEC == 4 ? m + 4 : m + 1, BST = VEC == 4 ? m16 + 4 : m16 + 1;
     const long long n = P.n;
     const bool ext = P.qids == nullptr;
     const long long q0 = P.q0;
@@ -233,11 +242,21 @@ __device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw)
         auto stage = [&](int s, int buf) {
             const int l = residue_order(s);
             float* dst = Bs + buf * kCT * BST;
-            for (int e = tid; e < kCT * m16; e += kThreads) {
-                int cj = e / m16, c = e - cj * m16;
-                long long g = j0 + cj;
-                if (g < cl) cp_async4(dst + cj * BST + c, P.vperm + g * m + l * m16 + c);
-                else dst[cj * BST + c] = 0.f;
+            if (VEC == 4) {
+                const int m4 = m16 >> 2;
+                for (int e = tid; e < kCT * m4; e += kThreads) {
+                    int cj = e / m4, c = (e - cj * m4) << 2;
+                    long long g = j0 + cj;
+                    if (g < cl) cp_async16(dst + cj * BST + c, P.vperm + g * m + l * m16 + c);
+                    else *(float4*)(dst + cj * BST + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            } else {
+                for (int e = tid; e < kCT * m16; e += kThreads) {
+                    int cj = e / m16, c = e - cj * m16;
+                    long long g = j0 + cj;
+                    if (g < cl) cp_async4(dst + cj * BST + c, P.vperm + g * m + l * m16 + c);
+                    else dst[cj * BST + c] = 0.f;
+                }
             }
             cp_async_commit();
         };
@@ -256,17 +275,39 @@ __device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw)
 #pragma unroll
                 for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
             const float* Ab = As + l * m16;
+            if (VEC == 4) {
+#pragma unroll 2
+                for (int c = 0; c < m16; c += 4) {
+                    float4 av[QPT], bv[4];
+#pragma unroll
+                    for (int a = 0; a < QPT; ++a) av[a] = *(const float4*)(Ab + (tq + 16 * a) * AST + c);
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) bv[b] = *(const float4*)(Bb + (tc + 16 * b) * BST + c);
+#pragma unroll
+                    for (int a = 0; a < QPT; ++a)
+#pragma unroll
+                        for (int b = 0; b < 4; ++b) {
+                            float t = acc[a][b];
+                            t = __fadd_rn(__fmul_rn(av[a].x, bv[b].x), t);
+                            t = __fadd_rn(__fmul_rn(av[a].y, bv[b].y), t);
+                            t = __fadd_rn(__fmul_rn(av[a].z, bv[b].z), t);
+                            t = __fadd_rn(__fmul_rn(av[a].w, bv[b].w), t);
+                            acc[a][b] = t;
+                        }
+                }
+            } else {
 #pragma unroll 4
-            for (int c = 0; c < m16; ++c) {
-                float av[QPT], bv[4];
+                for (int c = 0; c < m16; ++c) {
+                    float av[QPT], bv[4];
 #pragma unroll
-                for (int a = 0; a < QPT; ++a) av[a] = Ab[(tq + 16 * a) * AST + c];
+                    for (int a = 0; a < QPT; ++a) av[a] = Ab[(tq + 16 * a) * AST + c];
 #pragma unroll
-                for (int b = 0; b < 4; ++b) bv[b] = Bb[(tc + 16 * b) * BST + c];
+                    for (int b = 0; b < 4; ++b) bv[b] = Bb[(tc + 16 * b) * BST + c];
 #pragma unroll
-                for (int a = 0; a < QPT; ++a)
+                    for (int a = 0; a < QPT; ++a)
 #pragma unroll
-                    for (int b = 0; b < 4; ++b) acc[a][b] = __fadd_rn(__fmul_rn(av[a], bv[b]), acc[a][b]);
+                        for (int b = 0; b < 4; ++b) acc[a][b] = __fadd_rn(__fmul_rn(av[a], bv[b]), acc[a][b]);
+                }
             }
             // fold into the reduction tree
 #pragma unroll
@@ -348,6 +389,12 @@ __device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw)
         P.out_idx[g * P.out_stride + j] = ok ? (long long)Li[qi * k + j] : -1LL;
         P.out_dist[g * P.out_stride + j] = ok ? Ld[qi * k + j] : CT_FLT_MAX;
     }
+}
+
+template <int QT>
+__device__ __forceinline__ void run_tile(const Tile& P, unsigned char* smem_raw) {
+    if ((P.m & 63) == 0) run_tile_v<QT, 4>(P, smem_raw);
+    else run_tile_v<QT, 1>(P, smem_raw);
 }
 
 }  // namespace dense

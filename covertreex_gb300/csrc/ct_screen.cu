@@ -521,9 +521,9 @@ __device__ __forceinline__ unsigned long long pack_key(float d, int id) {
 struct RescoreParams {
     const float* v; int m;          // natural layout, dataset order
     const float* coords; int d;     // raw coordinates, dataset order
-    const double* inv_ls;           // FP64 1 / lengthscale
+    const float* inv_ls_df;         // 1 / lengthscale as double-float pairs (hi, lo) per axis
     const float* p;
-    double var; int kernel_type; int predecessor;
+    float var; int kernel_type; int predecessor;
     long long n;
     const int* slot_id; long long nslots;
     const int* surv; const int* surv_cnt;
@@ -535,6 +535,81 @@ struct RescoreParams {
     // each followed by its candidate parts, so neighbouring warps gather overlapping rows
     const int* order; int parts;
 };
+
+// ---------------------------------------------------------- double-float
+// A value is an unevaluated sum h + l of two floats with |l| <= ulp(h)/2 (about
+// 48 significant bits).  TwoSum / TwoProd (Knuth, Dekker) give the exact rounding
+// errors; products of pairs drop only l*l terms.  Used for the exact distance of a
+// rescored pair: the FP64-grade result at FP32 issue rates.
+struct df {
+    float h, l;
+};
+__device__ __forceinline__ df df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    return df{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z))};
+}
+__device__ __forceinline__ df df_fast(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return df{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ df df_add(df x, df y) {
+    const df s = df_two_sum(x.h, y.h);
+    return df_fast(s.h, __fadd_rn(s.l, __fadd_rn(x.l, y.l)));
+}
+__device__ __forceinline__ df df_neg(df x) { return df{-x.h, -x.l}; }
+__device__ __forceinline__ df df_mul(df x, df y) {
+    const float p = __fmul_rn(x.h, y.h);
+    float e = __fmaf_rn(x.h, y.h, -p);
+    e = __fmaf_rn(x.h, y.l, e);
+    e = __fmaf_rn(x.l, y.h, e);
+    return df_fast(p, e);
+}
+__device__ __forceinline__ df df_mulf(df x, float f) {
+    const float p = __fmul_rn(x.h, f);
+    const float e = __fmaf_rn(x.l, f, __fmaf_rn(x.h, f, -p));
+    return df_fast(p, e);
+}
+__device__ __forceinline__ df df_sqrt(df x) {  // one Newton step from sqrtf
+    if (!(x.h > 0.f)) return df{0.f, 0.f};
+    const float r = sqrtf(x.h);
+    const float sq = __fmul_rn(r, r);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(x.h, sq), __fmaf_rn(r, r, -sq)), x.l);
+    return df_fast(r, res / (2.f * r));
+}
+__device__ __forceinline__ df df_div(df a, df b) {  // two quotient digits
+    const float q0 = a.h / b.h;
+    const df r = df_add(a, df_neg(df_mulf(b, q0)));
+    return df_fast(q0, r.h / b.h);
+}
+__device__ __forceinline__ bool df_gt(df a, df b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+
+// Double-float constants split from their double values at compile time.
+#define CT_DF(x) df{(float)(x), (float)((x) - (double)(float)(x))}
+// 1/i!, i = 0..12, as (hi, lo)
+__constant__ float kInvFact[26] = {
+#define CT_IF(f) (float)(1.0 / (f)), (float)(1.0 / (f) - (double)(float)(1.0 / (f)))
+    CT_IF(1.0), CT_IF(1.0), CT_IF(2.0), CT_IF(6.0), CT_IF(24.0), CT_IF(120.0), CT_IF(720.0), CT_IF(5040.0),
+    CT_IF(40320.0), CT_IF(362880.0), CT_IF(3628800.0), CT_IF(39916800.0), CT_IF(479001600.0)
+#undef CT_IF
+};
+
+// e^x for x <= 0: x = n ln2 + r (|r| <= ln2/2, ln2 as a double-float pair), the
+// Taylor series of e^r to degree 12 (truncation < 2e-16) in double-float Horner form,
+// then the scaling by 2^n in two exact steps.
+__device__ __forceinline__ df df_exp(df x) {
+    if (x.h < -103.f) return df{0.f, 0.f};
+    const float n = rintf(__fmul_rn(x.h, 1.44269504088896341f));
+    const df ln2 = CT_DF(0.693147180559945309417);
+    const df r = df_add(x, df_neg(df_mulf(ln2, n)));
+    df p = df{kInvFact[24], kInvFact[25]};
+#pragma unroll
+    for (int i = 11; i >= 0; --i) p = df_add(df_mul(p, r), df{kInvFact[2 * i], kInvFact[2 * i + 1]});
+    const int ni = (int)n;
+    const int hh = ni / 2;
+    const float s1 = __int_as_float((hh + 127) << 23), s2 = __int_as_float((ni - hh + 127) << 23);
+    return df{__fmul_rn(__fmul_rn(p.h, s1), s2), __fmul_rn(__fmul_rn(p.l, s1), s2)};
+}
 
 // Compensated FP32 dot product pieces (TwoProd via FMA, TwoSum).  The warp
 // splits a row of m <= 1024 floats into 32 lane slices of m/32 contiguous
@@ -562,7 +637,7 @@ __device__ __forceinline__ void load_query_slice(const float* row, int m, float 
 // Dots of the query slice with NC candidate rows at once (independent loads in flight).
 template <int NC>
 __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, const int (&cid)[NC],
-                                          const float (&vq)[32], double (&out)[NC]) {
+                                          const float (&vq)[32], df (&out)[NC]) {
     const int lane = threadIdx.x & 31;
     const int per = m >> 5;
     float s[NC], comp[NC];
@@ -613,32 +688,43 @@ __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, co
             hi = t;
             lo = (lo + ol) + err;
         }
-        out[c] = (double)hi + (double)lo;
+        out[c] = df_fast(hi, lo);
     }
 }
 
-// FP64 kernel value, normalisation and square root for one pair (one lane).
-__device__ __forceinline__ float exact_from_dot(const RescoreParams& P, int q, int c, double dot) {
+// Exact residual distance of one pair from its double-float V dot product: the
+// kernel value from the f32 coordinates, the normalisation and the square root, in
+// double-float arithmetic (one lane per pair).
+__device__ __forceinline__ float exact_from_dot(const RescoreParams& P, int q, int c, df dot) {
     if (q == c) return 0.f;
-    double d2 = 0.0;
+    df d2 = df{0.f, 0.f};
     for (int a = 0; a < P.d; ++a) {
-        double t = ((double)P.coords[(size_t)q * P.d + a] - (double)P.coords[(size_t)c * P.d + a]) * P.inv_ls[a];
-        d2 += t * t;
+        const df t = df_two_sum(P.coords[(size_t)q * P.d + a], -P.coords[(size_t)c * P.d + a]);  // exact
+        const df u = df_mul(t, df{P.inv_ls_df[2 * a], P.inv_ls_df[2 * a + 1]});
+        d2 = df_add(d2, df_mul(u, u));
     }
-    double kv;
+    df kv;
     if (P.kernel_type == 0) {
-        kv = P.var * exp(-0.5 * d2);
+        kv = df_mulf(df_exp(df{-0.5f * d2.h, -0.5f * d2.l}), P.var);
     } else {
-        double a = sqrt(5.0) * sqrt(d2);
-        kv = P.var * (1.0 + a + a * a / 3.0) * exp(-a);
+        const df a = df_mul(df_sqrt(d2), CT_DF(2.23606797749978969641));
+        const df poly = df_add(df_add(df{1.f, 0.f}, a), df_mul(df_mul(a, a), CT_DF(1.0 / 3.0)));
+        kv = df_mulf(df_mul(poly, df_exp(df_neg(a))), P.var);
     }
-    double pp = (double)P.p[q] * (double)P.p[c];
-    double denom = sqrt(pp > 1e-18 ? pp : 1e-18);
-    double rho = (kv - dot) / denom;
-    rho = rho < -1.0 ? -1.0 : (rho > 1.0 ? 1.0 : rho);
-    double ds = 1.0 - fabs(rho);
-    return (float)(ds > 0.0 ? sqrt(ds) : 0.0);
+    const float pq = P.p[q], pc = P.p[c];
+    const float ph = __fmul_rn(pq, pc);
+    df pp = df_fast(ph, __fmaf_rn(pq, pc, -ph));  // exact product
+    const df floor18 = CT_DF(1e-18);
+    if (!df_gt(pp, floor18)) pp = floor18;
+    df rho = df_div(df_add(kv, df_neg(dot)), df_sqrt(pp));
+    if (rho.h < 0.f) rho = df_neg(rho);
+    if (rho.h > 1.f || (rho.h == 1.f && rho.l > 0.f)) rho = df{1.f, 0.f};
+    const df ds = df_add(df{1.f, 0.f}, df_neg(rho));
+    if (!(ds.h > 0.f)) return 0.f;
+    const df dist = df_sqrt(ds);
+    return __fadd_rn(dist.h, dist.l);
 }
+#undef CT_DF
 
 __device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& fill, int k, bool has,
                                                  unsigned long long key);
@@ -681,11 +767,11 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
             cid = use_full ? (int)ci
                            : (ci < c0 ? P.surv[(size_t)(2 * slot) * HALF_CAP + ci]
                                       : P.surv[(size_t)(2 * slot + 1) * HALF_CAP + (ci - c0)]);
-        double mydot = 0.0;
+        df mydot = df{0.f, 0.f};
         const int nb = (int)((count - base) < 32 ? (count - base) : 32);
         for (int t = 0; t < nb; t += 4) {
             int cc[4];
-            double dots[4];
+            df dots[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const int src = __shfl_sync(0xffffffffu, cid, (t + u) & 31);
@@ -759,10 +845,10 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, co
     for (long long base = b0; base < b1; base += 32) {
         const int nb = (int)((b1 - base) < 32 ? (b1 - base) : 32);
         const int cid = lane < nb ? (int)(base + lane) : -1;
-        double mydot = 0.0;
+        df mydot = df{0.f, 0.f};
         for (int t = 0; t < nb; t += 4) {
             int cc[4];
-            double dots[4];
+            df dots[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u) cc[u] = (t + u) < nb ? (int)(base + t + u) : -1;
             warp_dots<4>(P.v, P.m, cc, vql, dots);
@@ -844,6 +930,7 @@ struct State {
     long long* lvl_meta = nullptr;          // [nlevels][3]: size, row_off, rows_pad
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
     double* inv_ls64 = nullptr;
+    float* inv_ls_df = nullptr;             // (hi, lo) float pairs of 1 / lengthscale
     int* status = nullptr;
     double* bounds = nullptr;               // Hilbert quantisation frame of the dataset (min/max per axis)
     // query slab: rows [n, n + slab_cap) of the query-side arrays hold new points
@@ -1045,6 +1132,7 @@ void ct_tree::release_screen() {
     cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
     cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
+    cudaFree(S->inv_ls_df);
     cudaFree(S->bounds);
     if (S->slab_done) cudaEventDestroy(S->slab_done);
     delete S;
@@ -1087,6 +1175,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->isp, sizeof(float) * rows_q);
     A((void**)&S->xmax, sizeof(float) * rows_q);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
+    A((void**)&S->inv_ls_df, sizeof(float) * 128);
     A((void**)&S->status, sizeof(int));
     A((void**)&S->bounds, sizeof(double) * 2 * 64);
     if (e == cudaSuccess && T->slab_rows > 0) {
@@ -1130,6 +1219,12 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
         double ils[64];
         for (int i = 0; i < T->d; ++i) ils[i] = T->inv_ls_host64[i];
         e = cudaMemcpyAsync(S->inv_ls64, ils, sizeof(double) * T->d, cudaMemcpyHostToDevice, st);
+        float ils_df[128];
+        for (int i = 0; i < T->d; ++i) {
+            ils_df[2 * i] = (float)ils[i];
+            ils_df[2 * i + 1] = (float)(ils[i] - (double)ils_df[2 * i]);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(S->inv_ls_df, ils_df, sizeof(float) * 2 * T->d, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemsetAsync(S->status, 0, sizeof(int), st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host vectors above go out of scope
     }
@@ -1359,8 +1454,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (timing) cudaEventRecord(ev[3], st);
     // ---- rescoring (into the part lists when parts > 1)
     RescoreParams R{};
-    R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls = S->inv_ls64; R.p = p;
-    R.var = (double)var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
+    R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls_df = S->inv_ls_df; R.p = p;
+    R.var = var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
     R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list;
     R.nfull = 0;
     R.k = k; R.evals = evals_d;

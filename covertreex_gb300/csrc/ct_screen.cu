@@ -958,6 +958,47 @@ __global__ void inverse_perm_kernel(const int* order, long long n, int* inv) {
 // position inside its level.  Queries without a level sort last.
 constexpr int kBands = 16;
 constexpr int kWarmTiles = 16;  // nearest candidate tiles that set the thresholds before any pair is kept
+
+// A (query tile, part) unit of the sweep and the kernel that writes its jobs.
+struct JobUnit {
+    int qx;               // query tile of the A operand (t * parts + p)
+    int p, parts;
+    int cc, t0, ntl;      // level tiles [t0, t0 + ntl), spiral centre cc (ntl = 0: no level)
+    int lo_tile;          // dataset tiles from lo_tile follow the level tiles
+    int warm, count;      // warm-up jobs; all jobs
+    long long off;        // first job in the flat list
+};
+
+// w-th tile of the spiral cc, cc+1, cc-1, cc+2, cc-2, ... clipped to [t0, t0 + ntl)
+__device__ __forceinline__ int spiral_tile(const JobUnit& U, int w) {
+    if (w == 0) return U.cc;
+    const int left = U.cc - U.t0, right = U.t0 + U.ntl - 1 - U.cc;
+    const int mm = left < right ? left : right;
+    if (w <= 2 * mm) return (w & 1) ? U.cc + (w + 1) / 2 : U.cc - w / 2;
+    return right > left ? U.cc + (w - mm) : U.cc - (w - mm);
+}
+
+// Job i of a unit: i < warm: warm-up (heap only) over the part's i-th level tile;
+// otherwise the part's (i - warm)-th tile, marked when warm-up already fed its heap.
+// The part's tiles are entries p, p + parts, ... of the tile's list (spiral, then
+// dataset tiles).
+__global__ void gen_jobs_kernel(const JobUnit* __restrict__ units, Job* __restrict__ jobs) {
+    const JobUnit U = units[blockIdx.x];
+    for (int i = threadIdx.x; i < U.count; i += blockDim.x) {
+        const bool warmup = i < U.warm;
+        const int j = warmup ? i : i - U.warm;
+        const int w = U.p + j * U.parts;
+        int which, ctile;
+        if (w < U.ntl) {
+            ctile = spiral_tile(U, w);
+            which = warmup ? 2 : (j < U.warm ? 4 : 0);
+        } else {
+            ctile = U.lo_tile + (w - U.ntl);
+            which = 1;
+        }
+        jobs[U.off + i] = Job{U.qx, ctile, which, i == 0 ? 1 : 0};
+    }
+}
 __global__ void slot_ids_kernel(const long long* q, long long nq, long long n, int* slot_id,
                                 unsigned long long* key_lvl, int* val_lvl, const unsigned long long* hil_key,
                                 const unsigned long long* lvl_key, const long long* lvl_meta, int nlevels,
@@ -1266,6 +1307,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     long long* evals_d = nullptr;
     unsigned* qtau = nullptr;
     Job* jobs = nullptr;
+    JobUnit* units_d = nullptr;
     const int nbh = ct::radix_num_blocks(nq);
     auto A = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(p, bytes ? bytes : 16, st); };
     A((void**)&slot_id, sizeof(int) * nq);
@@ -1302,8 +1344,15 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form setup: %s", cudaGetErrorString(e));
 
-    // ---- per query tile: candidate tiles nearest-first
-    std::vector<std::vector<Job>> tiles(nqt);
+    // ---- per query tile: its candidate tiles nearest-first.  Tile t sweeps the
+    // level's Hilbert tiles in a spiral around its queries' position (cc, then
+    // cc+1, cc-1, cc+2, ... clipped to the level), then in predecessor mode the
+    // dataset tiles [lo_tile, hi_tile) that hold ids beyond the level.
+    struct TileSpec {
+        int cc, t0, ntl, lo_tile, hi_tile;
+    };
+    std::vector<TileSpec> spec(nqt, TileSpec{0, 0, 0, 0, 0});
+    std::vector<char> busy(nqt, 0);
     const long long n_ds_tiles = S->rows_pad / TC;
     for (long long t = 0; t < nqt; ++t) {
         long long maxq = -1;
@@ -1317,27 +1366,24 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         };
         long long row = row_of(r);
         if (row < 0) row = row_of(t * TQ);
-        std::vector<Job>& J = tiles[t];
         int li = -1;
         if (row >= 0)
             for (int l = 0; l < nlev; ++l)
                 if (row >= S->levels[l].row_off && row < S->levels[l].row_off + S->levels[l].rows_pad) li = l;
+        TileSpec& sp = spec[t];
         if (li >= 0) {
             const Level& L = S->levels[li];
-            const long long t0 = L.row_off / TC, ntl = L.rows_pad / TC;
-            const long long cc = std::min(std::max(row / TC, t0), t0 + ntl - 1);
-            J.push_back(Job{(int)t, (int)cc, 0, 0});
-            for (long long dlt = 1; dlt < ntl; ++dlt) {
-                if (cc + dlt < t0 + ntl) J.push_back(Job{(int)t, (int)(cc + dlt), 0, 0});
-                if (cc - dlt >= t0) J.push_back(Job{(int)t, (int)(cc - dlt), 0, 0});
-            }
+            sp.t0 = (int)(L.row_off / TC);
+            sp.ntl = (int)(L.rows_pad / TC);
+            sp.cc = (int)std::min<long long>(std::max<long long>(row / TC, sp.t0), sp.t0 + sp.ntl - 1);
         }
         if (predecessor) {
             // ids >= the level size are not in the level: sweep them in dataset order
-            long long lo_tile = (li >= 0 && li < nlev - 1) ? S->levels[li].size / TC : (li == nlev - 1 ? n_ds_tiles : 0);
-            long long hi_tile = std::min((maxq + TC - 1) / TC, n_ds_tiles);
-            for (long long c = lo_tile; c < hi_tile; ++c) J.push_back(Job{(int)t, (int)c, 1, 0});
+            sp.lo_tile = (int)((li >= 0 && li < nlev - 1) ? S->levels[li].size / TC : (li == nlev - 1 ? n_ds_tiles : 0));
+            sp.hi_tile = (int)std::min((maxq + TC - 1) / TC, n_ds_tiles);
+            if (sp.hi_tile < sp.lo_tile) sp.hi_tile = sp.lo_tile;
         }
+        busy[t] = (sp.ntl + sp.hi_tile - sp.lo_tile) > 0;
     }
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -1348,7 +1394,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     // merged at the end.  A part's threshold bounds the k-th distance within the
     // part, so its survivors still contain the part's true top k.
     long long busy_tiles = 0, max_jobs = 0;
-    for (const auto& J : tiles) if (!J.empty()) { ++busy_tiles; max_jobs = std::max<long long>(max_jobs, (long long)J.size()); }
+    for (long long t = 0; t < nqt; ++t)
+        if (busy[t]) { ++busy_tiles; max_jobs = std::max<long long>(max_jobs, spec[t].ntl + spec[t].hi_tile - spec[t].lo_tile); }
     int parts = 1;
     if (busy_tiles > 0 && busy_tiles < sms) {
         parts = (int)std::min<long long>(32, sms / busy_tiles);
@@ -1356,53 +1403,57 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     }
     const long long nslots = nq * parts;
     const long long rows_x = rows_q * parts;
-    // jobs of each (query tile, part): a heap-only warm-up over the part's first tiles,
-    // then every tile of the part with survivors kept
-    std::vector<std::vector<Job>> ptiles(nqt * parts);
+    // Units (query tile, part): a heap-only warm-up over the part's first level tiles,
+    // then every tile of the part (every parts-th of the tile's list) with survivors kept.
+    std::vector<JobUnit> units;
     for (long long t = 0; t < nqt; ++t) {
-        const std::vector<Job>& J = tiles[t];
-        if (J.empty()) continue;
+        if (!busy[t]) continue;
+        const TileSpec& sp = spec[t];
+        const int nJ = sp.ntl + sp.hi_tile - sp.lo_tile;
         for (int pp = 0; pp < parts; ++pp) {
-            std::vector<Job> mine;
-            for (size_t w = pp; w < J.size(); w += parts) mine.push_back(J[w]);
-            if (mine.empty()) continue;
-            const int qt = (int)(t * parts + pp);
-            std::vector<Job>& out = ptiles[qt];
-            size_t nlevel_jobs = 0;
-            for (const Job& jb : mine) if (!(jb.which & 1)) ++nlevel_jobs;
-            const int warm = (int)std::min<size_t>(parts > 1 ? std::max<size_t>(1, std::min<size_t>(kWarmTiles, nlevel_jobs / 4))
-                                                             : kWarmTiles, nlevel_jobs);
-            for (int w = 0; w < warm; ++w) out.push_back(Job{qt, mine[w].ctile, 2, 0});
-            for (size_t w = 0; w < mine.size(); ++w)
-                out.push_back(Job{qt, mine[w].ctile, mine[w].which | ((int)w < warm ? 4 : 0), 0});
-            out[0].first = 1;
+            const int mine = nJ > pp ? (nJ - pp + parts - 1) / parts : 0;
+            if (mine == 0) continue;
+            const int nlev_mine = sp.ntl > pp ? (sp.ntl - pp + parts - 1) / parts : 0;
+            const int warm = std::min(parts > 1 ? std::max(1, std::min(kWarmTiles, nlev_mine / 4)) : kWarmTiles,
+                                      nlev_mine);
+            JobUnit u;
+            u.qx = (int)(t * parts + pp); u.p = pp; u.parts = parts;
+            u.cc = sp.cc; u.t0 = sp.t0; u.ntl = sp.ntl; u.lo_tile = sp.lo_tile;
+            u.warm = warm; u.count = warm + mine; u.off = 0;
+            units.push_back(u);
         }
     }
-    // longest-processing-time assignment of (query tile, part) units to persistent CTAs
-    std::vector<long long> order;
-    for (long long t = 0; t < (long long)ptiles.size(); ++t) if (!ptiles[t].empty()) order.push_back(t);
-    std::sort(order.begin(), order.end(), [&](long long a, long long b) { return ptiles[a].size() > ptiles[b].size(); });
+    // longest-processing-time assignment of units to persistent CTAs
+    std::vector<int> order(units.size());
+    for (size_t i = 0; i < units.size(); ++i) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return units[a].count > units[b].count; });
     const int ncta = (int)std::min<long long>((long long)sms, (long long)order.size());
-    std::vector<std::vector<long long>> per_cta(ncta);
+    std::vector<std::vector<int>> per_cta(ncta);
     std::vector<std::pair<long long, int>> load;  // (jobs, cta) min-heap
     for (int c = 0; c < ncta; ++c) load.push_back({0, c});
     auto cmp = [](const std::pair<long long, int>& a, const std::pair<long long, int>& b) { return a.first > b.first; };
     std::make_heap(load.begin(), load.end(), cmp);
-    for (long long t : order) {
+    for (int u : order) {
         std::pop_heap(load.begin(), load.end(), cmp);
         auto& lc = load.back();
-        per_cta[lc.second].push_back(t);
-        lc.first += (long long)ptiles[t].size();
+        per_cta[lc.second].push_back(u);
+        lc.first += units[u].count;
         std::push_heap(load.begin(), load.end(), cmp);
     }
-    std::vector<Job> flat;
+    std::vector<JobUnit> flat_units;
     std::vector<int> begin(ncta + 1, 0);
+    long long njobs = 0;
     for (int c = 0; c < ncta; ++c) {
-        begin[c] = (int)flat.size();
-        for (long long t : per_cta[c]) flat.insert(flat.end(), ptiles[t].begin(), ptiles[t].end());
+        begin[c] = (int)njobs;
+        for (int u : per_cta[c]) {
+            JobUnit x = units[u];
+            x.off = njobs;
+            njobs += x.count;
+            flat_units.push_back(x);
+        }
     }
-    begin[ncta] = (int)flat.size();
-    const long long pairs_main = (long long)flat.size() * TQ * TC;  // every job runs its MMAs
+    begin[ncta] = (int)njobs;
+    const long long pairs_main = njobs * TQ * TC;  // every job runs its MMAs
     // part-expanded slots and A rows, the A operand, survivor lists
     const int* a_slot_use = a_slot_lvl;
     const int* rowmap_use = rowmap_lvl;
@@ -1425,12 +1476,20 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     A((void**)&surv, sizeof(int) * nslots * SURV_CAP);
     A((void**)&surv_cnt, sizeof(int) * 2 * nslots);
     A((void**)&full_list, sizeof(int) * nslots);
-    A((void**)&jobs, sizeof(Job) * (flat.size() + 1));
+    A((void**)&jobs, sizeof(Job) * (njobs + 1));
+    A((void**)&units_d, sizeof(JobUnit) * (flat_units.size() + 1));
     A((void**)&cta_begin, sizeof(int) * (ncta + 1));
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
     split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_use, rows_x, al_hi, al_lo);
     ++launches;
-    if (e == cudaSuccess && !flat.empty()) e = cudaMemcpyAsync(jobs, flat.data(), sizeof(Job) * flat.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !flat_units.empty()) {
+        e = cudaMemcpyAsync(units_d, flat_units.data(), sizeof(JobUnit) * flat_units.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            gen_jobs_kernel<<<(unsigned)flat_units.size(), 128, 0, st>>>(units_d, jobs);
+            e = cudaGetLastError();
+            ++launches;
+        }
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(cta_begin, begin.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * 2 * nslots, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(nfull_d, 0, sizeof(int), st);
@@ -1548,6 +1607,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
     cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st); cudaFreeAsync(qtau, st);
+    if (units_d) cudaFreeAsync(units_d, st);
     if (a_slot_x) cudaFreeAsync(a_slot_x, st);
     if (rowmap_x) cudaFreeAsync(rowmap_x, st);
     if (slot_id_x) cudaFreeAsync(slot_id_x, st);

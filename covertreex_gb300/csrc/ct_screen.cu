@@ -151,8 +151,9 @@ __device__ __forceinline__ void heap_push(float* h, int n, float x) {
 // bit 2 of `which`: a kept job whose candidate tile already fed the heap during warm-up
 __device__ __forceinline__ bool jb_warm_seen(const Job& jb) { return (jb.which & 4) != 0; }
 
-// DP: coordinates read per candidate (4 when D <= 4, else 8).
-template <int MODE, int DP>
+// DP: coordinates read per candidate (4 when D <= 4, else 8).  KT: kernel type (0 RBF,
+// 1 Matern 5/2) as a template parameter, so each group of 8 pairs is one basic block.
+template <int MODE, int DP, int KT>
 __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -385,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     const float axm = aq + meta.z;                      // 2.4e-7 (|x_q| + |x_c|)
                     const float ed2 = fmaf((dd + 2.f) * 5.97e-8f, d2, 0.5f * axm * fmaf(dd, d2, 1.f));
                     float kv, ek;
-                    if (P.kernel_type == 0) {
+                    if (KT == 0) {
                         kv = P.var * __expf(-0.5f * d2);
                         ek = kv * fmaf(6e-8f, d2, fmaf(0.5f, ed2, 1e-6f));
                     } else {
@@ -1147,18 +1148,16 @@ static cudaError_t launch_sweep(const MMAParams& P, int mode, int ncta, cudaStre
     const size_t smem = smem_layout(P.k, P.nstages).total;
     cudaError_t e;
     if (mode == MODE_DEBUG) {
-        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_DEBUG, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_DEBUG, 8, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        screen_sweep_kernel<MODE_DEBUG, 8><<<ncta, kThreads, smem, st>>>(P);
-    } else if (P.d <= 4) {
-        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        screen_sweep_kernel<MODE_SWEEP, 4><<<ncta, kThreads, smem, st>>>(P);
-    } else {
-        e = cudaFuncSetAttribute(screen_sweep_kernel<MODE_SWEEP, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        screen_sweep_kernel<MODE_SWEEP, 8><<<ncta, kThreads, smem, st>>>(P);
+        screen_sweep_kernel<MODE_DEBUG, 8, 0><<<ncta, kThreads, smem, st>>>(P);
+        return cudaGetLastError();
     }
+    void (*fn)(MMAParams) = P.d <= 4 ? (P.kernel_type == 0 ? screen_sweep_kernel<MODE_SWEEP, 4, 0> : screen_sweep_kernel<MODE_SWEEP, 4, 1>)
+                                     : (P.kernel_type == 0 ? screen_sweep_kernel<MODE_SWEEP, 8, 0> : screen_sweep_kernel<MODE_SWEEP, 8, 1>);
+    e = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fn<<<ncta, kThreads, smem, st>>>(P);
     return cudaGetLastError();
 }
 

@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     }
                     const float R = fabsf(kv - v[i]);
                     const float e = fmaf(vnq, meta.x, ek) + fmaf(R, 1.2e-7f, 1e-30f);
-                    const bool valid = cid >= 0 && !(P.predecessor && cid >= qid);
+                    const bool valid = (cid >= 0) & !((P.predecessor != 0) & (cid >= qid));
                     const float inf = __int_as_float(0x7f800000);
                     blo[i] = !valid ? -inf : (cid == qid ? inf : (R - e) * meta.y);
                     bhi[i] = !valid ? -inf : (cid == qid ? inf : (R + e) * meta.y);
@@ -405,7 +405,13 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 }
                 // Phase 2: survivors and heap against the current thresholds.  Phase 1's
                 // values do not depend on the thresholds, so this keeps and heaps exactly
-                // the pairs that pair-by-pair processing would.
+                // the pairs that pair-by-pair processing would.  Most groups have no pair
+                // to keep or heap; one test skips them (the thresholds then stay as they are).
+                bool any = false;
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    any |= (keep_job & (bhi[i] >= thr_keep)) | (feed_heap & (blo[i] > thr_heap));
+                if (!any) continue;
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     if (keep_job && bhi[i] >= thr_keep) {

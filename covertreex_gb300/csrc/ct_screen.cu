@@ -268,18 +268,21 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) break;
                 float* r = recs + (size_t)acc * TC * REC;
                 const int* bid = P.b_id[jb.which & 1];
+                // Columns 2i and 2i+1 share one record of 2 * REC floats with their fields
+                // interleaved (field f of column c at 2f + (c & 1)), so that the epilogue
+                // computes both pairs with one packed f32x2 instruction per step.
                 for (int e = lane; e < TC; e += 32) {
                     const int cid = bid[(long long)jb.ctile * TC + e];
-                    float* o = r + e * REC;
+                    float* o = r + (e >> 1) * (2 * REC) + (e & 1);
                     if (cid >= 0) {
 #pragma unroll
-                        for (int c = 0; c < kMaxD; ++c) o[c] = c < P.d ? P.xs[(size_t)cid * P.d + c] : 0.f;
-                        o[8] = P.err_coef * P.vn[cid]; o[9] = P.isp[cid]; o[10] = 2.4e-7f * P.xmax[cid];
-                        o[11] = __int_as_float(cid);
+                        for (int c = 0; c < kMaxD; ++c) o[2 * c] = c < P.d ? P.xs[(size_t)cid * P.d + c] : 0.f;
+                        o[16] = P.err_coef * P.vn[cid]; o[18] = P.isp[cid]; o[20] = 2.4e-7f * P.xmax[cid];
+                        o[22] = __int_as_float(cid);
                     } else {
 #pragma unroll
-                        for (int c = 0; c < 11; ++c) o[c] = 0.f;
-                        o[11] = __int_as_float(-1);
+                        for (int c = 0; c < 11; ++c) o[2 * c] = 0.f;
+                        o[22] = __int_as_float(-1);
                     }
                 }
                 __syncwarp();
@@ -301,14 +304,16 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         int slot = -1, qid = -1, hn = 0, cnt = 0;
         unsigned gen = 0;  // query-tile generation, tags the shared row threshold
         float tau2 = 1.f;
-        float xq[kMaxD];
+        float nxq[kMaxD];  // negated query coordinates: x_c + (-x_q) is the rounded x_c - x_q
         float vnq = 0.f, isq = 0.f, aq = 0.f;
+        int lim = 0;       // a candidate id is valid iff (unsigned)cid < (unsigned)lim
         // keep the pair iff (R + e) * isc >= thr_keep; it may enter the heap iff
         // (R - e) * isc > thr_heap (both derived from tau2 / the heap top; see below)
         float thr_keep = 0.f, thr_heap = 0.f;
 #pragma unroll
-        for (int c = 0; c < kMaxD; ++c) xq[c] = 0.f;
+        for (int c = 0; c < kMaxD; ++c) nxq[c] = 0.f;
         const float dd = (float)P.d;
+        const float ced2 = (dd + 2.f) * 5.97e-8f;
         for (int j = jb0; j < jb1; ++j, ++lt) {
             const Job jb = P.jobs[j];
             const int acc = lt & 1;
@@ -322,7 +327,9 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 if (qid >= 0) {
                     vnq = P.vn[qid]; isq = P.isp[qid]; aq = 2.4e-7f * P.xmax[qid];
 #pragma unroll
-                    for (int c = 0; c < kMaxD; ++c) xq[c] = c < P.d ? P.xs[(size_t)qid * P.d + c] : 0.f;
+                    for (int c = 0; c < kMaxD; ++c) nxq[c] = c < P.d ? -P.xs[(size_t)qid * P.d + c] : 0.f;
+                    // predecessor mode: 0 <= cid < qid; otherwise cid >= 0 (ids stay below INT_MAX)
+                    lim = P.predecessor ? qid : 0x7fffffff;
                 }
                 thr_keep = 0.f;   // tau2 = 1: keep everything
                 thr_heap = -CT_FLT_MAX;  // heap not full: every pair enters
@@ -363,45 +370,59 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 float blo[8], bhi[8];
                 int bid[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const float4* r4 = (const float4*)(rb + (col0 + i) * REC);
-                    const float4 meta = r4[2];
-                    const int cid = __float_as_int(meta.w);
-                    const float4 xa = r4[0];
-                    float d2 = 0.f, t;
-                    t = xq[0] - xa.x; d2 = fmaf(t, t, d2);
-                    t = xq[1] - xa.y; d2 = fmaf(t, t, d2);
-                    t = xq[2] - xa.z; d2 = fmaf(t, t, d2);
-                    t = xq[3] - xa.w; d2 = fmaf(t, t, d2);
-                    if (DP > 4) {
-                        const float4 xb = r4[1];
-                        t = xq[4] - xb.x; d2 = fmaf(t, t, d2);
-                        t = xq[5] - xb.y; d2 = fmaf(t, t, d2);
-                        t = xq[6] - xb.z; d2 = fmaf(t, t, d2);
-                        t = xq[7] - xb.w; d2 = fmaf(t, t, d2);
+                for (int i = 0; i < 4; ++i) {
+                    // columns col0 + 2i (.x) and col0 + 2i + 1 (.y)
+                    const float4* r4 = (const float4*)(rb + ((col0 >> 1) + i) * (2 * REC));
+                    const float4 m0 = r4[4];  // err_coef * |v_c|, 1/sqrt(p_c)
+                    const float4 m1 = r4[5];  // 2.4e-7 max|x_c|, id
+                    const float2 err = make_float2(m0.x, m0.y), isc = make_float2(m0.z, m0.w);
+                    float2 d2 = make_float2(0.f, 0.f), t;
+#pragma unroll
+                    for (int h = 0; h < DP / 2; ++h) {
+                        const float4 x = r4[h];
+                        t = __fadd2_rn(make_float2(x.x, x.y), make_float2(nxq[2 * h], nxq[2 * h]));
+                        d2 = __ffma2_rn(t, t, d2);
+                        t = __fadd2_rn(make_float2(x.z, x.w), make_float2(nxq[2 * h + 1], nxq[2 * h + 1]));
+                        d2 = __ffma2_rn(t, t, d2);
                     }
                     // Certified error of the kernel value.  d2 error: (D+2) 2^-24 d2 from the
                     // sum plus 2^-22 sum|dx| (|x_q| + |x_c|) from the scaled coordinates, with
                     // sum|dx| <= sqrt(D d2) <= (D d2 + 1) / 2.
-                    const float axm = aq + meta.z;                      // 2.4e-7 (|x_q| + |x_c|)
-                    const float ed2 = fmaf((dd + 2.f) * 5.97e-8f, d2, 0.5f * axm * fmaf(dd, d2, 1.f));
-                    float kv, ek;
+                    const float2 axm = __fadd2_rn(make_float2(aq, aq), make_float2(m1.x, m1.y));
+                    const float2 u = __ffma2_rn(make_float2(dd, dd), d2, make_float2(1.f, 1.f));
+                    const float2 ed2 =
+                        __ffma2_rn(make_float2(ced2, ced2), d2, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), axm), u));
+                    float2 kv, ek;
                     if (KT == 0) {
-                        kv = P.var * __expf(-0.5f * d2);
-                        ek = kv * fmaf(6e-8f, d2, fmaf(0.5f, ed2, 1e-6f));
+                        const float2 h = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);
+                        kv = __fmul2_rn(make_float2(P.var, P.var), make_float2(__expf(h.x), __expf(h.y)));
+                        const float2 f = __ffma2_rn(make_float2(6e-8f, 6e-8f), d2,
+                                                    __ffma2_rn(make_float2(0.5f, 0.5f), ed2, make_float2(1e-6f, 1e-6f)));
+                        ek = __fmul2_rn(kv, f);
                     } else {
-                        const float a = 2.2360679775f * sqrtf(d2);
-                        const float ea = __expf(-a);
-                        kv = P.var * (1.f + a + a * a * 0.33333334f) * ea;
-                        ek = kv * (1e-6f + 2.4e-7f * a) + P.var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
+                        const float aa = 2.2360679775f * sqrtf(d2.x), ab = 2.2360679775f * sqrtf(d2.y);
+                        const float ea = __expf(-aa), eb = __expf(-ab);
+                        kv.x = P.var * (1.f + aa + aa * aa * 0.33333334f) * ea;
+                        kv.y = P.var * (1.f + ab + ab * ab * 0.33333334f) * eb;
+                        ek.x = kv.x * (1e-6f + 2.4e-7f * aa) + P.var * (0.8334f * ed2.x + 1e-7f * aa * aa) * (1.f + aa) * ea;
+                        ek.y = kv.y * (1e-6f + 2.4e-7f * ab) + P.var * (0.8334f * ed2.y + 1e-7f * ab * ab) * (1.f + ab) * eb;
                     }
-                    const float R = fabsf(kv - v[i]);
-                    const float e = fmaf(vnq, meta.x, ek) + fmaf(R, 1.2e-7f, 1e-30f);
-                    const bool valid = (cid >= 0) & !((P.predecessor != 0) & (cid >= qid));
+                    const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
+                    const float2 R = make_float2(fabsf(dif.x), fabsf(dif.y));
+                    const float2 e = __fadd2_rn(__ffma2_rn(make_float2(vnq, vnq), err, ek),
+                                                __ffma2_rn(R, make_float2(1.2e-7f, 1.2e-7f), make_float2(1e-30f, 1e-30f)));
+                    const float2 lo = __fmul2_rn(__fadd2_rn(R, make_float2(-e.x, -e.y)), isc);
+                    const float2 hi = __fmul2_rn(__fadd2_rn(R, e), isc);
+                    // +inf for the query itself, -inf for padding and predecessor-violating pairs
+                    const int ca = __float_as_int(m1.z), cb = __float_as_int(m1.w);
+                    const bool va = (unsigned)ca < (unsigned)lim, vb = (unsigned)cb < (unsigned)lim;
                     const float inf = __int_as_float(0x7f800000);
-                    blo[i] = !valid ? -inf : (cid == qid ? inf : (R - e) * meta.y);
-                    bhi[i] = !valid ? -inf : (cid == qid ? inf : (R + e) * meta.y);
-                    bid[i] = cid;
+                    blo[2 * i] = !va ? -inf : (ca == qid ? inf : lo.x);
+                    bhi[2 * i] = !va ? -inf : (ca == qid ? inf : hi.x);
+                    blo[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : lo.y);
+                    bhi[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : hi.y);
+                    bid[2 * i] = ca;
+                    bid[2 * i + 1] = cb;
                 }
                 // Phase 2: survivors and heap against the current thresholds.  Phase 1's
                 // values do not depend on the thresholds, so this keeps and heaps exactly

@@ -524,11 +524,14 @@ __global__ void point_scalars_kernel(const float* __restrict__ v, const float* _
 
 // ------------------------------------------------------------------ selection
 // Bitonic sort of RBUF 64-bit keys held in shared memory by one warp.
-__device__ void warp_bitonic_sort(unsigned long long* keys) {
+// Sorts keys[0, len) for a power of two len <= RBUF; callers keep every entry at or
+// beyond their fill count at ~0 (the largest key), so sorting the smallest power of
+// two that covers the fill orders the whole buffer.
+__device__ void warp_bitonic_sort(unsigned long long* keys, int len = RBUF) {
     const int lane = threadIdx.x & 31;
-    for (int k = 2; k <= RBUF; k <<= 1) {
+    for (int k = 2; k <= len; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = lane; i < RBUF; i += 32) {
+            for (int i = lane; i < len; i += 32) {
                 int ixj = i ^ j;
                 if (ixj > i) {
                     unsigned long long a = keys[i], b = keys[ixj];
@@ -539,6 +542,12 @@ __device__ void warp_bitonic_sort(unsigned long long* keys) {
             __syncwarp();
         }
     }
+}
+
+__device__ __forceinline__ int sort_len(int fill) {
+    int len = 32;
+    while (len < fill && len < RBUF) len <<= 1;
+    return len;
 }
 
 __device__ __forceinline__ unsigned long long pack_key(float d, int id) {
@@ -562,6 +571,7 @@ struct RescoreParams {
     // visiting order of the survivor pass: query slots in the sweep's (Hilbert) order,
     // each followed by its candidate parts, so neighbouring warps gather overlapping rows
     const int* order; int parts;
+    int chunk;  // candidates per item of the exhaustive pass (parts == 1)
 };
 
 // ---------------------------------------------------------- double-float
@@ -814,7 +824,7 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
         evals += nb;
         warp_topk_append(keys, fill, k, ci < count, pack_key(mydist, cid));
     }
-    warp_bitonic_sort(keys);
+    warp_bitonic_sort(keys, sort_len(fill));
     for (int j = lane; j < k; j += 32) {
         unsigned long long key = keys[j];
         bool ok = key != ~0ULL;
@@ -825,8 +835,8 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
 }
 
 // Exhaustive rescoring of overflowed queries, split for parallelism: each warp
-// scores one chunk of a query's candidate range and keeps its k best keys.
-constexpr int kChunk = 4096;
+// scores one chunk of a query's candidate range (P.chunk ids, sized to the work so
+// that a few overflowed queries still spread over the SMs) and keeps its k best keys.
 struct ChunkItem {
     int slot, chunk;
 };
@@ -867,8 +877,8 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, co
     for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
     __syncwarp();
     const long long count = P.predecessor ? (long long)q : P.n;
-    const long long b0 = (long long)it.chunk * kChunk;
-    const long long b1 = b0 + kChunk < count ? b0 + kChunk : count;
+    const long long b0 = (long long)it.chunk * P.chunk;
+    const long long b1 = b0 + P.chunk < count ? b0 + P.chunk : count;
     int fill = k;
     for (long long base = b0; base < b1; base += 32) {
         const int nb = (int)((b1 - base) < 32 ? (b1 - base) : 32);
@@ -887,7 +897,7 @@ __global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, co
         const float dist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
         warp_topk_append(keys, fill, k, lane < nb, pack_key(dist, cid));
     }
-    warp_bitonic_sort(keys);
+    warp_bitonic_sort(keys, sort_len(fill));
     for (int j = lane; j < k; j += 32) partial[(size_t)wi * k + j] = keys[j];
     if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)(b1 - b0));
 }
@@ -911,7 +921,7 @@ __global__ void merge_chunks_kernel(RescoreParams P, const int* item_begin, cons
         const unsigned long long key = has ? partial[base + lane] : ~0ULL;
         warp_topk_append(keys, fill, k, has && key != ~0ULL, key);
     }
-    warp_bitonic_sort(keys);
+    warp_bitonic_sort(keys, sort_len(fill));
     for (int j = lane; j < k; j += 32) {
         const unsigned long long key = keys[j];
         const bool ok = key != ~0ULL;
@@ -957,6 +967,7 @@ struct State {
     unsigned long long* lvl_key = nullptr;  // row -> Hilbert key (UINT64_MAX padding)
     long long* lvl_meta = nullptr;          // [nlevels][3]: size, row_off, rows_pad
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
+    unsigned* isp_max = nullptr;            // bits of max 1/sqrt(p) over the dataset rows
     double* inv_ls64 = nullptr;
     float* inv_ls_df = nullptr;             // (hi, lo) float pairs of 1 / lengthscale
     int* status = nullptr;
@@ -1004,6 +1015,62 @@ __device__ __forceinline__ int spiral_tile(const JobUnit& U, int w) {
     const int mm = left < right ? left : right;
     if (w <= 2 * mm) return (w & 1) ? U.cc + (w + 1) / 2 : U.cc - w / 2;
     return right > left ? U.cc + (w - mm) : U.cc - (w - mm);
+}
+
+// Exhaustive rescoring of an overflowed part slot over its own candidates only: the
+// part's share of its query tile's list (spiral entries p, p + parts, ... of the
+// level tiles, then the dataset tiles), tpc tiles per item.  The part's exact top k
+// then joins the other parts' lists in the k-way merge.
+struct PartItem {
+    int slot, unit, j0;
+};
+__global__ void rescore_part_kernel(RescoreParams P, const PartItem* __restrict__ items, int nitems, int tpc,
+                                    const JobUnit* __restrict__ units, const int* __restrict__ lvl_id,
+                                    const int* __restrict__ ds_id, unsigned long long* __restrict__ partial) {
+    extern __shared__ unsigned long long pkeys_all[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long* keys = pkeys_all + (size_t)warp * RBUF;
+    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
+    if (w >= nitems) return;
+    const PartItem it = items[w];
+    const JobUnit U = units[it.unit];
+    const int q = P.slot_id[it.slot];
+    const int k = P.k;
+    float vql[32];
+    load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
+    for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
+    __syncwarp();
+    const int mine = U.count - U.warm;
+    const int j1 = it.j0 + tpc < mine ? it.j0 + tpc : mine;
+    int fill = k;
+    long long evals = 0;
+    for (int j = it.j0; j < j1; ++j) {
+        const int wt = U.p + j * U.parts;
+        const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                                    : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
+        for (int base = 0; base < TC; base += 32) {
+            int cid = ids[base + lane];
+            if (P.predecessor && cid >= q) cid = -1;
+            df mydot = df{0.f, 0.f};
+            for (int t = 0; t < 32; t += 4) {
+                int cc[4];
+                df dots[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) cc[u] = __shfl_sync(0xffffffffu, cid, t + u);
+                warp_dots<4>(P.v, P.m, cc, vql, dots);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (lane == t + u) mydot = dots[u];
+            }
+            const bool has = cid >= 0;
+            const float dist = has ? exact_from_dot(P, q, cid, mydot) : 0.f;
+            evals += __popc(__ballot_sync(0xffffffffu, has));
+            warp_topk_append(keys, fill, k, has, pack_key(dist, cid));
+        }
+    }
+    warp_bitonic_sort(keys, sort_len(fill));
+    for (int j = lane; j < k; j += 32) partial[(size_t)w * k + j] = keys[j];
+    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
 }
 
 // Job i of a unit: i < warm: warm-up (heap only) over the part's i-th level tile;
@@ -1068,6 +1135,78 @@ __global__ void slot_ids_kernel(const long long* q, long long nq, long long n, i
     key_lvl[i] = kl;
 }
 
+// Seeded thresholds.  Any k eligible candidates bound a query's k-th distance, so
+// before the sweep each query (one warp) scores exactly the S rows of its level
+// that surround its Hilbert position and starts its shared threshold qtau at the
+// k-th smallest of those d^2 = 1 - |rho|, plus a margin for the double-float error
+// of the exact distance (at most about 2e-12 / sqrt(p_q p_c) in rho).  Without it a
+// query far from the centre of a scattered query tile keeps every pair until its
+// own heap fills.  Level rows hold ids below the level size, which in predecessor
+// mode is at most the query id, so every seed is an eligible candidate.
+template <int S>
+__global__ void seed_tau_kernel(RescoreParams R, const unsigned long long* __restrict__ key_sorted,
+                                const int* __restrict__ val_sorted, long long nq, const int* __restrict__ lvl_id,
+                                const long long* __restrict__ lvl_meta, const unsigned* __restrict__ isp_max,
+                                unsigned* __restrict__ qtau) {
+    const int lane = threadIdx.x & 31;
+    const long long w = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (w >= nq) return;
+    const unsigned long long key = key_sorted[w];
+    const unsigned group = (unsigned)(key >> 32);
+    if (group >= 0xFFFFFFFEu) return;  // no level
+    const int i = val_sorted[w];
+    const int q = R.slot_id[i];
+    if (q < 0) return;
+    const int li = (int)(group / kBands);
+    const long long size = lvl_meta[3 * li], off = lvl_meta[3 * li + 1];
+    if (size < R.k) return;
+    long long start = (long long)(key & 0xFFFFFFFFULL) - off - S / 2;
+    if (start > size - S) start = size - S;
+    if (start < 0) start = 0;
+    const int cnt = size < S ? (int)size : S;
+    float vql[32];
+    load_query_slice(R.v + (size_t)q * R.m, R.m, vql);
+    float dist[S / 32];
+#pragma unroll
+    for (int r = 0; r < S / 32; ++r) {
+        const int cid = r * 32 + lane < cnt ? lvl_id[off + start + r * 32 + lane] : -1;
+        df mydot = df{0.f, 0.f};
+        for (int t = 0; t < 32; t += 4) {
+            int cc[4];
+            df dots[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) cc[u] = __shfl_sync(0xffffffffu, cid, t + u);
+            warp_dots<4>(R.v, R.m, cc, vql, dots);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (lane == t + u) mydot = dots[u];
+        }
+        dist[r] = cid >= 0 ? exact_from_dot(R, q, cid, mydot) : __int_as_float(0x7f800000);
+    }
+    // k-th smallest distance: bisection over the bit patterns (non-negative floats
+    // order as unsigned integers)
+    unsigned lo = 0, hi = 0x7f800000u;
+    while (lo < hi) {
+        const unsigned mid = lo + ((hi - lo) >> 1);
+        int c = 0;
+#pragma unroll
+        for (int r = 0; r < S / 32; ++r) c += __popc(__ballot_sync(0xffffffffu, __float_as_uint(dist[r]) <= mid));
+        if (c >= R.k) hi = mid; else lo = mid + 1;
+    }
+    if (lane == 0 && lo < 0x7f800000u) {
+        const float dk = __uint_as_float(lo);
+        const float isq = rsqrtf(fmaxf(R.p[q], 1e-30f)) * 1.01f;
+        const float margin = 4e-12f * fminf(isq * __uint_as_float(*isp_max) * 1.01f, 1e9f) + 1e-12f;
+        const float t2 = fminf(__fadd_ru(__fmul_ru(__fmul_ru(dk, dk), 1.000004f), margin), 1.f);
+        atomicMin(&qtau[i], __float_as_uint(t2));
+    }
+}
+
+__global__ void max_bits_kernel(const float* __restrict__ x, long long n, unsigned* __restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) atomicMax(out, __float_as_uint(fabsf(x[i])));
+}
+
 // rowmap (A row -> dataset row) and a_slot (A row -> slot) from a sorted slot list
 __global__ void arows_kernel(const int* sorted_slots, long long nq, long long rows, const int* slot_id, int* a_slot,
                              int* rowmap) {
@@ -1102,29 +1241,15 @@ __global__ void expand_slots_kernel(const int* slot_id, long long nq, int parts,
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < nq * parts) slot_id_x[i] = slot_id[i / parts];
 }
-// One warp per query: the exact top-k over its parts.  A part slot that overflowed
-// was rescored against every candidate, so its list is already the answer;
-// otherwise the parts cover disjoint candidates and their lists are k-way merged
-// (lane p holds the head of part p).
+// One warp per query: the exact top-k over its parts.  The parts cover disjoint
+// candidates (an overflowed part was rescored over its own candidates only), so
+// their lists are k-way merged (lane p holds the head of part p).
 __global__ void merge_parts_kernel(const long long* __restrict__ pidx, const float* __restrict__ pdist,
-                                   const int* __restrict__ surv_cnt, long long nq, int parts, int k,
+                                   long long nq, int parts, int k,
                                    long long* __restrict__ out_idx, float* __restrict__ out_dist) {
     const long long q = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (q >= nq) return;
-    int full = -1;
-    for (int pp = 0; pp < parts; ++pp) {
-        const long long sl = q * parts + pp;
-        if (surv_cnt[2 * sl] > HALF_CAP || surv_cnt[2 * sl + 1] > HALF_CAP) { full = pp; break; }
-    }
-    if (full >= 0) {
-        const long long sl = q * parts + full;
-        for (int j = lane; j < k; j += 32) {
-            out_idx[q * k + j] = pidx[sl * k + j];
-            out_dist[q * k + j] = pdist[sl * k + j];
-        }
-        return;
-    }
     const float kInf = __int_as_float(0x7f800000);
     int pos = 0;
     float hd = kInf;
@@ -1199,7 +1324,7 @@ void ct_tree::release_screen() {
     cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
     cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
-    cudaFree(S->inv_ls_df);
+    cudaFree(S->inv_ls_df); cudaFree(S->isp_max);
     cudaFree(S->bounds);
     if (S->slab_done) cudaEventDestroy(S->slab_done);
     delete S;
@@ -1241,6 +1366,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->vn, sizeof(float) * rows_q);
     A((void**)&S->isp, sizeof(float) * rows_q);
     A((void**)&S->xmax, sizeof(float) * rows_q);
+    A((void**)&S->isp_max, sizeof(unsigned));
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->inv_ls_df, sizeof(float) * 128);
     A((void**)&S->status, sizeof(int));
@@ -1257,7 +1383,9 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
         iota_kernel<<<grid_for(S->rows_pad), 256, 0, st>>>(S->b_id_ds, S->rows_pad, n);
         split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->b_id_ds, S->rows_pad, S->ds_hi, S->ds_lo);
         point_scalars_kernel<<<grid_for(n), 256, 0, st>>>(T->vnat, T->p, T->xs, n, m, T->d, S->vn, S->isp, S->xmax);
-        e = cudaGetLastError();
+        e = cudaMemsetAsync(S->isp_max, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) max_bits_kernel<<<grid_for(n), 256, 0, st>>>(S->isp, n, S->isp_max);
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(order_h.data(), S->hil_order, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(key_h.data(), S->hil_key, 8 * n, cudaMemcpyDeviceToHost, st);
@@ -1363,6 +1491,23 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         arows_kernel<<<grid_for(rows_q), 256, 0, st>>>(val_lvl, nq, rows_q, slot_id, a_slot_lvl, rowmap_lvl);
         e = cudaGetLastError();
     }
+    // seeded thresholds, when scoring S candidates per query costs less than the
+    // exhaustive rescoring of a few overflowed queries would
+    const int seed_s = k <= 32 ? 64 : 128;
+    const bool seeded = (long long)seed_s * nq <= 16LL * n;
+    if (e == cudaSuccess && seeded) {
+        RescoreParams Rs{};
+        Rs.v = vnat; Rs.m = m; Rs.coords = coords_raw; Rs.d = d; Rs.inv_ls_df = S->inv_ls_df; Rs.p = p;
+        Rs.var = var; Rs.kernel_type = kernel_type; Rs.predecessor = predecessor ? 1 : 0; Rs.n = n;
+        Rs.slot_id = slot_id; Rs.nslots = nq; Rs.k = k;
+        const unsigned grid = (unsigned)((nq + 7) / 8);
+        if (seed_s == 64)
+            seed_tau_kernel<64><<<grid, 256, 0, st>>>(Rs, key_lvl, val_lvl, nq, S->lvl_id, S->lvl_meta, S->isp_max, qtau);
+        else
+            seed_tau_kernel<128><<<grid, 256, 0, st>>>(Rs, key_lvl, val_lvl, nq, S->lvl_id, S->lvl_meta, S->isp_max, qtau);
+        e = cudaGetLastError();
+        ++launches;
+    }
     std::vector<unsigned long long> hk_lvl(nq);
     std::vector<int> hrow_id(rows_q);
     if (e == cudaSuccess) e = cudaMemcpyAsync(hk_lvl.data(), key_lvl, 8 * nq, cudaMemcpyDeviceToHost, st);
@@ -1440,7 +1585,9 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             const int mine = nJ > pp ? (nJ - pp + parts - 1) / parts : 0;
             if (mine == 0) continue;
             const int nlev_mine = sp.ntl > pp ? (sp.ntl - pp + parts - 1) / parts : 0;
-            const int warm = std::min(parts > 1 ? std::max(1, std::min(kWarmTiles, nlev_mine / 4)) : kWarmTiles,
+            // seeded queries start from a tight threshold: two warm-up tiles fill the heaps
+            const int warm_cap = seeded ? 2 : kWarmTiles;
+            const int warm = std::min(parts > 1 ? std::max(1, std::min(warm_cap, nlev_mine / 4)) : warm_cap,
                                       nlev_mine);
             JobUnit u;
             u.qx = (int)(t * parts + pp); u.p = pp; u.parts = parts;
@@ -1542,7 +1689,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls_df = S->inv_ls_df; R.p = p;
     R.var = var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
     R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list;
-    R.nfull = 0;
+    R.nfull = 0; R.chunk = 4096;
     R.k = k; R.evals = evals_d;
     R.order = val_lvl; R.parts = parts;
     R.out_idx = parts > 1 ? part_idx : (long long*)out_idx;
@@ -1561,41 +1708,90 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, S->status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     ChunkItem* items_d = nullptr;
+    PartItem* pitems_d = nullptr;
     int* item_begin_d = nullptr;
     int* perm_d = nullptr;
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess && nfull > 0) {
-        // split every overflowed slot's exhaustive range into chunks
+        // Split every overflowed slot's exhaustive range into items, about 24 warps'
+        // worth per SM in all (at most 4096 candidates per item).
+        const long long target_items = (long long)sms * 24;
         std::vector<int> fl(nfull), sid(nslots);
         e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id_use, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st);
+        std::vector<int> sorted_q;
+        if (parts > 1) {
+            sorted_q.resize(nq);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(sorted_q.data(), val_lvl, sizeof(int) * nq, cudaMemcpyDeviceToHost, st);
+        }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         std::sort(fl.begin(), fl.end());
-        std::vector<ChunkItem> items;
         std::vector<int> ibeg(nfull + 1, 0);
-        for (int i = 0; i < nfull; ++i) {
-            ibeg[i] = (int)items.size();
-            const long long count = predecessor ? (long long)sid[fl[i]] : n;
-            for (long long c = 0; c * kChunk < count; ++c) items.push_back(ChunkItem{fl[i], (int)c});
+        int nitems = 0;
+        std::vector<ChunkItem> items;
+        std::vector<PartItem> pitems;
+        std::vector<int> perm;
+        int tpc = 1;
+        if (parts > 1) {
+            // slot s*parts + pp of query s: its A tile, then the unit (tile, part)
+            std::vector<int> tile_of(nq, -1), unit_of(nqt * parts, -1);
+            for (long long r = 0; r < nq; ++r) tile_of[sorted_q[r]] = (int)(r / TQ);
+            for (size_t u = 0; u < flat_units.size(); ++u) unit_of[flat_units[u].qx] = (int)u;
+            long long total_tiles = 0;
+            std::vector<int> fu(nfull, -1);
+            for (int i = 0; i < nfull; ++i) {
+                const int qi = fl[i] / parts, pp = fl[i] % parts;
+                fu[i] = unit_of[(long long)tile_of[qi] * parts + pp];
+                if (fu[i] >= 0) total_tiles += flat_units[fu[i]].count - flat_units[fu[i]].warm;
+            }
+            tpc = (int)std::min<long long>(16, std::max<long long>(1, (total_tiles + target_items - 1) / target_items));
+            for (int i = 0; i < nfull; ++i) {
+                ibeg[i] = (int)pitems.size();
+                if (fu[i] < 0) continue;
+                const int mine = flat_units[fu[i]].count - flat_units[fu[i]].warm;
+                for (int j0 = 0; j0 < mine; j0 += tpc) pitems.push_back(PartItem{fl[i], fu[i], j0});
+            }
+            ibeg[nfull] = (int)pitems.size();
+            nitems = (int)pitems.size();
+        } else {
+            long long total = 0;
+            for (int i = 0; i < nfull; ++i) total += predecessor ? (long long)sid[fl[i]] : n;
+            R.chunk = (int)std::min<long long>(4096, std::max<long long>(256, ((total + target_items - 1) / target_items + 255) / 256 * 256));
+            for (int i = 0; i < nfull; ++i) {
+                ibeg[i] = (int)items.size();
+                const long long count = predecessor ? (long long)sid[fl[i]] : n;
+                for (long long c = 0; c * R.chunk < count; ++c) items.push_back(ChunkItem{fl[i], (int)c});
+            }
+            ibeg[nfull] = (int)items.size();
+            nitems = (int)items.size();
+            perm.resize(nitems);
+            for (int i = 0; i < nitems; ++i) perm[i] = i;
+            std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return items[a].chunk < items[b].chunk; });
         }
-        ibeg[nfull] = (int)items.size();
-        const int nitems = (int)items.size();
-        std::vector<int> perm(nitems);
-        for (int i = 0; i < nitems; ++i) perm[i] = i;
-        std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return items[a].chunk < items[b].chunk; });
-        A((void**)&items_d, sizeof(ChunkItem) * (nitems + 1));
-        A((void**)&perm_d, sizeof(int) * (nitems + 1));
         A((void**)&item_begin_d, sizeof(int) * (nfull + 1));
         A((void**)&partial, sizeof(unsigned long long) * ((size_t)nitems * k + 1));
+        if (parts > 1) {
+            A((void**)&pitems_d, sizeof(PartItem) * (nitems + 1));
+            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(pitems_d, pitems.data(), sizeof(PartItem) * nitems, cudaMemcpyHostToDevice, st);
+        } else {
+            A((void**)&items_d, sizeof(ChunkItem) * (nitems + 1));
+            A((void**)&perm_d, sizeof(int) * (nitems + 1));
+            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(items_d, items.data(), sizeof(ChunkItem) * nitems, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(perm_d, perm.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, st);
+        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(items_d, items.data(), sizeof(ChunkItem) * nitems, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(perm_d, perm.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, st);
         R.nfull = nfull;
         if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_part_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(merge_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (e == cudaSuccess && nitems > 0) {
-            rescore_chunk_kernel<<<(unsigned)((nitems + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, items_d, perm_d, nitems, partial);
+            const unsigned grid = (unsigned)((nitems + rwpb - 1) / rwpb);
+            if (parts > 1)
+                rescore_part_kernel<<<grid, 32 * rwpb, rsmem, st>>>(R, pitems_d, nitems, tpc, units_d, S->lvl_id,
+                                                                   S->b_id_ds, partial);
+            else
+                rescore_chunk_kernel<<<grid, 32 * rwpb, rsmem, st>>>(R, items_d, perm_d, nitems, partial);
             merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, item_begin_d, partial);
             e = cudaGetLastError();
             launches += 2;
@@ -1604,7 +1800,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
     if (e == cudaSuccess && parts > 1) {
-        merge_parts_kernel<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(part_idx, part_dist, surv_cnt, nq, parts, k,
+        merge_parts_kernel<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(part_idx, part_dist, nq, parts, k,
                                                                      (long long*)out_idx, out_dist);
         e = cudaGetLastError();
         ++launches;
@@ -1640,6 +1836,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (part_idx) cudaFreeAsync(part_idx, st);
     if (part_dist) cudaFreeAsync(part_dist, st);
     if (items_d) cudaFreeAsync(items_d, st);
+    if (pitems_d) cudaFreeAsync(pitems_d, st);
     if (perm_d) cudaFreeAsync(perm_d, st);
     if (item_begin_d) cudaFreeAsync(item_begin_d, st);
     if (partial) cudaFreeAsync(partial, st);

@@ -115,7 +115,8 @@ def estimate_tree_bytes(n: int, d: int, m: int) -> int:
 
 class ServingEngine:
     def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 2, max_step_points: int = 16384,
-                 dense_pair_limit: float = 1.0e11, device=None, reserve=(256, 3, 64)):
+                 max_step_work: float = 2.0e10, dense_pair_limit: float = 1.0e10, device=None,
+                 reserve=(256, 3, 64)):
         import torch
 
         from .device import CudaBatch
@@ -126,6 +127,7 @@ class ServingEngine:
         self.device = torch.device(device if device is not None else "cuda")
         self.budget = float(hbm_budget_bytes)
         self.max_step_points = int(max_step_points)
+        self.max_step_work = float(max_step_work)         # sum of Q * N * m per dense step
         self.dense_pair_limit = float(dense_pair_limit)   # Q * N * m at or below which a query runs dense
         self.trees: Dict[int, ResidentTree] = {}
         self.used_bytes = 0
@@ -133,16 +135,18 @@ class ServingEngine:
         self.peak_bytes = 0
         self.rejected: set = set()
         self.evicted: set = set()
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        # Query work runs on high-priority streams and builds on a low-priority one, so
+        # the block scheduler hands SMs freed by a build's kernels to queued query kernels.
+        self.streams = [torch.cuda.Stream(self.device, priority=-1) for _ in range(slots)]
         self.batches = [CudaBatch(self.device) for _ in range(slots)]
         for b in self.batches:
             b.reserve(*reserve)
-        self.build_stream = torch.cuda.Stream(self.device)
+        self.build_stream = torch.cuda.Stream(self.device, priority=0)
         self._build_in: "queue.Queue" = queue.Queue()
         self._build_out: "queue.Queue" = queue.Queue()
         self._worker = threading.Thread(target=self._build_worker, daemon=True)
         self._worker.start()
-        self.screen_stream = torch.cuda.Stream(self.device)
+        self.screen_stream = torch.cuda.Stream(self.device, priority=-1)
         self._screen_in: "queue.Queue" = queue.Queue()
         self._screen_out: "queue.Queue" = queue.Queue()
         self._screener = threading.Thread(target=self._screened_worker, daemon=True)
@@ -394,7 +398,7 @@ class ServingEngine:
                     progressed = True
             # admit queries: large ones to the screened worker, the rest into a free step slot
             if pending_queries:
-                take, keep, rows = [], [], 0
+                take, keep, rows, work = [], [], 0, 0.0
                 slot_free = bool(free_slots)
                 for q in pending_queries:
                     rec = recs[q.rid]
@@ -413,10 +417,13 @@ class ServingEngine:
                         screened_inflight += 1
                         self._screen_in.put((rec, q, tree))
                         continue
-                    if not slot_free or (rows > 0 and rows + q.points.shape[0] > self.max_step_points):
+                    w = float(q.points.shape[0]) * tree.n * tree.m
+                    if not slot_free or (rows > 0 and (rows + q.points.shape[0] > self.max_step_points
+                                                       or work + w > self.max_step_work)):
                         keep.append(q)
                         continue
                     rows += q.points.shape[0]
+                    work += w
                     rec.start = now
                     take.append((rec, q, tree))
                 pending_queries = keep

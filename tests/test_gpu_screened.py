@@ -94,6 +94,21 @@ def test_screened_mixture_d8_subset(cuda_available):
     assert np.array_equal(gi2[::-1], gi)
 
 
+@pytest.mark.parametrize("predecessor", [False, True])
+def test_screened_scattered_small_id_set(cuda_available, predecessor):
+    """A few scattered query ids (candidate parts, seeded thresholds) including
+    inducing rows (p ~ 1e-6: overflowed part slots rescored over their part's
+    candidates only), against FP64."""
+    case = gaussian_case(30000, 3, 256, 1, 1.0, seed=11)
+    idx = _index(case)
+    r = np.random.default_rng(12)
+    q = np.concatenate([r.choice(30000, 40, replace=False), case["inducing"][:8]]).astype(np.int64)
+    gi, gd = idx.knn(q, 50, predecessor=predecessor, form="screened")
+    if not predecessor:  # every candidate is eligible: the inducing rows' part slots overflow
+        assert idx.last_stats["overflow_queries"] > 0
+    _check_against_fp64(case, q, 50, predecessor, gi, gd)
+
+
 def test_screened_predecessor_invariants(cuda_available):
     case = gaussian_case(300, 2, 32, 0, 1.0, seed=42)
     idx = _index(case)

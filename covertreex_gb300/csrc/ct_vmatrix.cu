@@ -5,7 +5,8 @@
 //                                    pairwise differences of FP64 coordinates
 //   L   = chol(Kmm)                  blocked right-looking (32-column panels):
 //                                    diagonal factor / panel solve / trailing update
-//   Li  = L^-1                       column-wise forward substitution
+//   Li  = L^-1                       column-wise forward substitution, one warp
+//                                    per column
 //   V   = K(X, Z) Li^T               in row chunks: K(X_c, Z) evaluated into a
 //                                    scratch buffer, then an FP64 GEMM that only
 //                                    visits t <= j (Li is lower triangular)
@@ -20,6 +21,8 @@
 // the GEMM is register-tiled 64 x 64 with 4 x 4 outputs per thread and is bound by
 // the DFMA rate; N m^2 FMAs for N rows.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <math.h>
 
 #include "ct_vmatrix.h"
@@ -128,17 +131,29 @@ __global__ void zero_upper_kernel(double* __restrict__ A, int m) {
     if (j > i) A[e] = 0.0;
 }
 
-// Li = L^-1 (lower triangular): thread c solves L x = e_c by forward substitution.
-__global__ void trinv_kernel(const double* __restrict__ L, int m, double* __restrict__ Li) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// Li = L^-1 (lower triangular): warp c solves L x = e_c by forward substitution.
+// The lanes split each row's dot product (lane l takes t = c + l, c + l + 32, ...,
+// then a butterfly sum) and x stays in shared memory, so a column costs m - c
+// short steps instead of (m - c)^2 / 2 dependent FMAs on one thread.
+__global__ void __launch_bounds__(128) trinv_kernel(const double* __restrict__ L, int m, double* __restrict__ Li) {
+    extern __shared__ double trinv_x[];  // [warps per block][m]
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int c = blockIdx.x * (blockDim.x >> 5) + wib;
     if (c >= m) return;
-    for (int i = 0; i < c; ++i) Li[(size_t)i * m + c] = 0.0;
+    double* x = trinv_x + (size_t)wib * m;
+    for (int i = lane; i < m; i += 32) x[i] = 0.0;
+    __syncwarp();
     for (int i = c; i < m; ++i) {
-        double s = (i == c) ? 1.0 : 0.0;
         const double* Lrow = L + (size_t)i * m;
-        for (int t = c; t < i; ++t) s -= Lrow[t] * Li[(size_t)t * m + c];
-        Li[(size_t)i * m + c] = s / Lrow[i];
+        double s = 0.0;
+        for (int t = c + lane; t < i; t += 32) s = fma(Lrow[t], x[t], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const double xi = ((i == c ? 1.0 : 0.0) - s) / Lrow[i];
+        if (lane == 0) x[i] = xi;
+        __syncwarp();
     }
+    for (int i = lane; i < m; i += 32) Li[(size_t)i * m + c] = x[i];
 }
 
 // Kc[r][t] = K(x_{r0+r}, z_t) for r < rows.
@@ -249,7 +264,14 @@ cudaError_t vmatrix_factor(const double* z, int m, int d, int kt, double var, do
         }
     }
     zero_upper_kernel<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(L, m);
-    trinv_kernel<<<(m + 63) / 64, 64, 0, st>>>(L, m, Li);
+    // up to 4 warps per block, each with an m-double column in shared memory (m <= 16384)
+    const int tw = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / (sizeof(double) * (size_t)m)));
+    const size_t tsm = sizeof(double) * tw * (size_t)m;
+    if (tsm > 48 * 1024) {
+        e = cudaFuncSetAttribute(trinv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
+        if (e != cudaSuccess) return e;
+    }
+    trinv_kernel<<<(m + tw - 1) / tw, 32 * tw, tsm, st>>>(L, m, Li);
     return cudaGetLastError();
 }
 

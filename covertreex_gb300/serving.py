@@ -116,7 +116,7 @@ def estimate_tree_bytes(n: int, d: int, m: int) -> int:
 class ServingEngine:
     def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 2, max_step_points: int = 16384,
                  max_step_work: float = 2.0e10, dense_pair_limit: float = 1.0e10, device=None,
-                 reserve=(256, 3, 64)):
+                 reserve=(256, 3, 64), build_workers: int = 1):
         import torch
 
         from .device import CudaBatch
@@ -141,11 +141,16 @@ class ServingEngine:
         self.batches = [CudaBatch(self.device) for _ in range(slots)]
         for b in self.batches:
             b.reserve(*reserve)
-        self.build_stream = torch.cuda.Stream(self.device, priority=0)
+        # Builds are chains of small kernels with host synchronisations between them;
+        # with build_workers > 1 several run at once, each on its own thread and stream
+        # (more build throughput near saturation, a higher query p99 below it).
+        self.build_streams = [torch.cuda.Stream(self.device, priority=0) for _ in range(max(1, build_workers))]
         self._build_in: "queue.Queue" = queue.Queue()
         self._build_out: "queue.Queue" = queue.Queue()
-        self._worker = threading.Thread(target=self._build_worker, daemon=True)
-        self._worker.start()
+        self._workers = [threading.Thread(target=self._build_worker, args=(st,), daemon=True)
+                         for st in self.build_streams]
+        for w in self._workers:
+            w.start()
         self.screen_stream = torch.cuda.Stream(self.device, priority=-1)
         self._screen_in: "queue.Queue" = queue.Queue()
         self._screen_out: "queue.Queue" = queue.Queue()
@@ -154,7 +159,7 @@ class ServingEngine:
         self.launches = 0
 
     # ------------------------------------------------------------------ builds
-    def _build_tree(self, req: BuildRequest) -> ResidentTree:
+    def _build_tree(self, req: BuildRequest, st=None) -> ResidentTree:
         torch = self.torch
         from .device import CudaResidualIndex, CudaVFactor
 
@@ -162,7 +167,7 @@ class ServingEngine:
         X = np.ascontiguousarray(req.coords, dtype=np.float32)
         n, d = X.shape
         idx = inducing_indices(n, req.inducing_count, req.seed)
-        st = self.build_stream
+        st = self.build_streams[0] if st is None else st
         with torch.cuda.device(self.device), torch.cuda.stream(st):
             xd = torch.as_tensor(X, device=self.device)
             f = CudaVFactor(X[idx].astype(np.float64), kernel_type=req.kernel_type, variance=req.variance,
@@ -178,14 +183,14 @@ class ServingEngine:
         nbytes = index.device_bytes() + f.device_bytes()
         return ResidentTree(req.rid, index, f, n, d, index.m, nbytes, time.perf_counter() - t0)
 
-    def _build_worker(self):
+    def _build_worker(self, st):
         while True:
             item = self._build_in.get()
             if item is None:
                 return
             req, rec, est = item
             try:
-                tree = self._build_tree(req)
+                tree = self._build_tree(req, st)
                 self._build_out.put((req, rec, est, tree, None))
             except Exception as exc:  # reported through the record
                 self._build_out.put((req, rec, est, None, exc))
@@ -322,7 +327,7 @@ class ServingEngine:
         pending_queries: List[QueryRequest] = []
         inflight: List[_Step] = []
         free_slots = list(range(len(self.streams)))
-        worker_busy = False
+        builds_inflight = 0
         screened_inflight = 0
         t0 = time.perf_counter()
         i = 0
@@ -342,7 +347,7 @@ class ServingEngine:
                     req, rec, est, tree, exc = self._build_out.get_nowait()
                 except queue.Empty:
                     break
-                worker_busy = False
+                builds_inflight -= 1
                 progressed = True
                 self.reserved_bytes -= est
                 rec.done = time.perf_counter() - t0
@@ -375,7 +380,7 @@ class ServingEngine:
                     free_slots.append(step.slot)
                     progressed = True
             # admit a build
-            if not worker_busy and pending_builds:
+            if builds_inflight < len(self._workers) and pending_builds:
                 req = pending_builds[0]
                 n, d = req.coords.shape
                 est = estimate_tree_bytes(n, d, min(req.inducing_count, n))
@@ -393,7 +398,7 @@ class ServingEngine:
                     rec.start = now
                     self.reserved_bytes += est
                     self.peak_bytes = max(self.peak_bytes, self.used_bytes + self.reserved_bytes)
-                    worker_busy = True
+                    builds_inflight += 1
                     self._build_in.put((req, rec, est))
                     progressed = True
             # admit queries: large ones to the screened worker, the rest into a free step slot
@@ -491,9 +496,11 @@ class ServingEngine:
         return out
 
     def close(self):
-        self._build_in.put(None)
+        for _ in self._workers:
+            self._build_in.put(None)
         self._screen_in.put(None)
-        self._worker.join(timeout=30)
+        for w in self._workers:
+            w.join(timeout=30)
         self._screener.join(timeout=30)
         for t in list(self.trees.values()):
             t.index.free()

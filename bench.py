@@ -486,20 +486,6 @@ def main():
                      "call": float(np.mean([s["device_ms"] for s in stats]))},
     }
 
-    # ---- CPU baseline (rank 0, N=1 only): restated rust-hilbert on host cores
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        try:
-            subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
-            threads = os.cpu_count() or 1
-            qps, tree = oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False)
-            cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                   "sample": f"{min(args.cpu_sample, wl.n)} random query ids of the same workload, default budget "
-                             f"mode; tree build {tree.build_seconds:.2f} s excluded"}
-        except Exception as exc:  # the baseline is reported, never required
-            cpu = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"unavailable: {exc}"}
-
     batching = None
     serving = None
     if rank == 0 and world == 1 and not args.no_batching:
@@ -513,6 +499,21 @@ def main():
                                     args.serving_seconds)
         except Exception as exc:
             serving = {"unavailable": repr(exc)}
+
+    # ---- CPU baseline (rank 0, N=1 only): restated rust-hilbert on host cores, last,
+    # so that its OpenMP thread pool does not share the host with the serving loop
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
+            threads = os.cpu_count() or 1
+            qps, tree = oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False)
+            cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                   "sample": f"{min(args.cpu_sample, wl.n)} random query ids of the same workload, default budget "
+                             f"mode; tree build {tree.build_seconds:.2f} s excluded"}
+        except Exception as exc:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"unavailable: {exc}"}
 
     if rank == 0:
         line = {

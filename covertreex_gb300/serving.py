@@ -29,6 +29,8 @@ least-recently-used first.
 """
 from __future__ import annotations
 
+import contextlib
+import gc
 import queue
 import threading
 import time
@@ -99,6 +101,17 @@ class _Step:
     items: list = field(default_factory=list)   # (record, idx_host, dist_host, _, _)
     trees: list = field(default_factory=list)
     buffers: tuple = ()
+
+
+@contextlib.contextmanager
+def _gc_paused():
+    enabled = gc.isenabled()
+    gc.disable()
+    try:
+        yield
+    finally:
+        if enabled:
+            gc.enable()
 
 
 def estimate_tree_bytes(n: int, d: int, m: int) -> int:
@@ -318,7 +331,13 @@ class ServingEngine:
     def serve(self, requests: List[object], *, realtime: bool = True, time_limit: Optional[float] = None
               ) -> List[RequestRecord]:
         """Serve `requests` (arrival times in seconds from the start) and return one
-        record per request.  realtime=False admits everything at t=0."""
+        record per request.  realtime=False admits everything at t=0.  Python's cyclic
+        garbage collector is suspended for the length of the loop: a full collection in
+        a process holding many objects stalls the loop for tens of milliseconds."""
+        with _gc_paused():
+            return self._serve(requests, realtime=realtime, time_limit=time_limit)
+
+    def _serve(self, requests: List[object], *, realtime: bool, time_limit: Optional[float]) -> List[RequestRecord]:
         reqs = sorted(requests, key=lambda r: r.arrival)
         recs = {r.rid: RequestRecord(r.rid, "build" if isinstance(r, BuildRequest) else "query", r.arrival,
                                      (r.coords.shape[0] if isinstance(r, BuildRequest) else r.points.shape[0]))
@@ -455,7 +474,13 @@ class ServingEngine:
                           time_limit: Optional[float] = None) -> List[RequestRecord]:
         """Baseline: the plain per-request form.  One request at a time in arrival
         order, each query embedded and searched alone with the dense form, each
-        build done inline; nothing is batched or overlapped."""
+        build done inline; nothing is batched or overlapped (garbage collection
+        suspended as in serve())."""
+        with _gc_paused():
+            return self._serve_per_request(requests, realtime=realtime, time_limit=time_limit)
+
+    def _serve_per_request(self, requests: List[object], *, realtime: bool,
+                           time_limit: Optional[float]) -> List[RequestRecord]:
         torch = self.torch
         reqs = sorted(requests, key=lambda r: r.arrival)
         out = []

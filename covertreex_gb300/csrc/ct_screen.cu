@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "ct_common.cuh"
@@ -61,8 +62,7 @@ constexpr int kThreads = 96 + kEpiThreads;  // producer, MMA issuer, staging, ep
 constexpr int kMaxD = 8;
 constexpr int kMaxK = 64;                   // heap capacity per epilogue thread
 constexpr int REC = 12;                     // floats per staged candidate record
-constexpr int SURV_CAP = 1024;
-constexpr int HALF_CAP = SURV_CAP / 2;  // survivor segment per (query, column half)
+constexpr int kSurvCap = 1024;  // default survivors per query slot (two column halves)
 constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
 
 enum Mode { MODE_DEBUG = 0, MODE_SWEEP = 1 };
@@ -102,6 +102,7 @@ struct MMAParams {
     int nstages;
     float* out_f;        // debug output
     int* surv; int* surv_cnt;
+    int half_cap;        // survivor segment per (slot, column half)
     int* status;
     unsigned* qtau;      // per query (slot / parts): the smallest part threshold, float bits
     int parts;           // candidate parts per query (slots s*parts .. s*parts+parts-1)
@@ -436,7 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     if (keep_job && bhi[i] >= thr_keep) {
-                        if (cnt < HALF_CAP) P.surv[((size_t)slot * 2 + half) * HALF_CAP + cnt] = bid[i];
+                        if (cnt < P.half_cap) P.surv[((size_t)slot * 2 + half) * P.half_cap + cnt] = bid[i];
                         ++cnt;
                     }
                     if (feed_heap && blo[i] > thr_heap) {
@@ -563,7 +564,7 @@ struct RescoreParams {
     float var; int kernel_type; int predecessor;
     long long n;
     const int* slot_id; long long nslots;
-    const int* surv; const int* surv_cnt;
+    const int* surv; const int* surv_cnt; int half_cap;
     const int* full_slots; int nfull;  // slots rescored against every valid candidate
     int k;
     long long* out_idx; float* out_dist;
@@ -783,7 +784,7 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
                               : (P.order ? P.order[w / P.parts] * P.parts + (int)(w % P.parts) : (int)w);
     const int c0 = use_full ? 0 : P.surv_cnt[2 * slot];
     const int c1 = use_full ? 0 : P.surv_cnt[2 * slot + 1];
-    if (!use_full && (c0 > HALF_CAP || c1 > HALF_CAP)) return;  // handled by the exhaustive pass
+    if (!use_full && (c0 > P.half_cap || c1 > P.half_cap)) return;  // handled by the exhaustive pass
     const int q = P.slot_id[slot];
     if (q < 0) {
         for (int j = lane; j < P.k; j += 32) { P.out_idx[(size_t)slot * P.k + j] = -1; P.out_dist[(size_t)slot * P.k + j] = CT_FLT_MAX; }
@@ -803,8 +804,8 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
         int cid = -1;
         if (ci < count)
             cid = use_full ? (int)ci
-                           : (ci < c0 ? P.surv[(size_t)(2 * slot) * HALF_CAP + ci]
-                                      : P.surv[(size_t)(2 * slot + 1) * HALF_CAP + (ci - c0)]);
+                           : (ci < c0 ? P.surv[(size_t)(2 * slot) * P.half_cap + ci]
+                                      : P.surv[(size_t)(2 * slot + 1) * P.half_cap + (ci - c0)]);
         df mydot = df{0.f, 0.f};
         const int nb = (int)((count - base) < 32 ? (count - base) : 32);
         for (int t = 0; t < nb; t += 4) {
@@ -930,11 +931,11 @@ __global__ void merge_chunks_kernel(RescoreParams P, const int* item_begin, cons
     }
 }
 
-__global__ void collect_overflow_kernel(const int* __restrict__ surv_cnt, long long nslots, int* __restrict__ list,
-                                        int* __restrict__ nlist) {
+__global__ void collect_overflow_kernel(const int* __restrict__ surv_cnt, long long nslots, int half_cap,
+                                        int* __restrict__ list, int* __restrict__ nlist) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= nslots) return;
-    if (surv_cnt[2 * s] > HALF_CAP || surv_cnt[2 * s + 1] > HALF_CAP) list[atomicAdd(nlist, 1)] = (int)s;
+    if (surv_cnt[2 * s] > half_cap || surv_cnt[2 * s + 1] > half_cap) list[atomicAdd(nlist, 1)] = (int)s;
 }
 
 
@@ -1573,6 +1574,14 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         parts = (int)std::max<long long>(1, std::min<long long>(parts, max_jobs / 8));
     }
     const long long nslots = nq * parts;
+    // Survivor lists per slot: kSurvCap by default (CT_SCREEN_SURVIVOR_CAP overrides it,
+    // within 8 GiB for the call); a slot that overflows is rescored exhaustively.
+    int half_cap = kSurvCap / 2;
+    if (const char* env = std::getenv("CT_SCREEN_SURVIVOR_CAP")) {
+        const long long want = std::atoll(env) / 2;
+        const long long fit = (8LL << 30) / (8LL * std::max<long long>(nslots, 1));
+        half_cap = (int)std::max<long long>(64, std::min<long long>({want, fit, 1LL << 20}));
+    }
     const long long rows_x = rows_q * parts;
     // Units (query tile, part): a heap-only warm-up over the part's first level tiles,
     // then every tile of the part (every parts-th of the tile's list) with survivors kept.
@@ -1646,7 +1655,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         a_slot_use = a_slot_x; rowmap_use = rowmap_x; slot_id_use = slot_id_x;
     }
     A((void**)&al_hi, sizeof(bf16) * rows_x * m); A((void**)&al_lo, sizeof(bf16) * rows_x * m);
-    A((void**)&surv, sizeof(int) * nslots * SURV_CAP);
+    A((void**)&surv, sizeof(int) * nslots * 2 * (size_t)half_cap);
     A((void**)&surv_cnt, sizeof(int) * 2 * nslots);
     A((void**)&full_list, sizeof(int) * nslots);
     A((void**)&jobs, sizeof(Job) * (njobs + 1));
@@ -1680,7 +1689,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     P.xs = xs; P.d = d; P.vn = S->vn; P.isp = S->isp; P.xmax = S->xmax;
     P.var = var; P.kernel_type = kernel_type; P.predecessor = predecessor ? 1 : 0;
     P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
-    P.surv = surv; P.surv_cnt = surv_cnt; P.status = S->status;
+    P.surv = surv; P.surv_cnt = surv_cnt; P.half_cap = half_cap; P.status = S->status;
     P.qtau = qtau; P.parts = parts;
     if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
     if (timing) cudaEventRecord(ev[3], st);
@@ -1688,7 +1697,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     RescoreParams R{};
     R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls_df = S->inv_ls_df; R.p = p;
     R.var = var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
-    R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.full_slots = full_list;
+    R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.half_cap = half_cap;
+    R.full_slots = full_list;
     R.nfull = 0; R.chunk = 4096;
     R.k = k; R.evals = evals_d;
     R.order = val_lvl; R.parts = parts;
@@ -1699,7 +1709,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
     if (e == cudaSuccess) {
         rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 0);
-        collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, full_list, nfull_d);
+        collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, half_cap, full_list, nfull_d);
         e = cudaGetLastError();
         launches += 2;
     }

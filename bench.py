@@ -511,6 +511,15 @@ def main():
             cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                    "sample": f"{min(args.cpu_sample, wl.n)} random query ids of the same workload, default budget "
                              f"mode; tree build {tree.build_seconds:.2f} s excluded"}
+            del tree
+            # the reference's parity mode (COVERTREEX_RESIDUAL_PARITY=1: no budget ladder,
+            # exhaustive up to the cover-radius prune), reported separately
+            pq = max(16, args.cpu_sample // 32)
+            qps_p, tree_p = oracle_queries_per_s(wl, pq, threads, parity=True)
+            cpu["parity_mode"] = {"value": qps_p, "unit": "queries/s", "cores": threads,
+                                  "sample": f"{min(pq, wl.n)} random query ids, parity mode; tree build "
+                                            f"{tree_p.build_seconds:.2f} s excluded"}
+            del tree_p
         except Exception as exc:  # the baseline is reported, never required
             cpu = {"value": None, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"unavailable: {exc}"}

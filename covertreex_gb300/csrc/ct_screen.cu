@@ -103,6 +103,7 @@ struct MMAParams {
     float* out_f;        // debug output
     int* surv; int* surv_cnt;
     int half_cap;        // survivor segment per (slot, column half)
+    const float* rec[2]; // candidate records in tile order (levels, dataset), TC * REC floats per tile
     int* status;
     unsigned* qtau;      // per query (slot / parts): the smallest part threshold, float bits
     int parts;           // candidate parts per query (slots s*parts .. s*parts+parts-1)
@@ -259,35 +260,19 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             sm::mbar_wait(done, 0, P.status, 14);
         }
     } else if (warp == 2) {
-        // ------------------------------------------------------------ candidate staging
-        if (MODE == MODE_SWEEP) {
+        // ------------------------------------------------------------ candidate records
+        // One bulk copy per job brings the candidate tile's records (built once per tree
+        // in tile order by build_records_kernel) into the free record buffer.
+        if (MODE == MODE_SWEEP && lane == 0) {
             int lt = 0;
             for (int j = jb0; j < jb1; ++j, ++lt) {
                 const Job jb = P.jobs[j];
                 const int acc = lt & 1;
                 const unsigned aph = (unsigned)((lt >> 1) & 1);
                 if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) break;
-                float* r = recs + (size_t)acc * TC * REC;
-                const int* bid = P.b_id[jb.which & 1];
-                // Columns 2i and 2i+1 share one record of 2 * REC floats with their fields
-                // interleaved (field f of column c at 2f + (c & 1)), so that the epilogue
-                // computes both pairs with one packed f32x2 instruction per step.
-                for (int e = lane; e < TC; e += 32) {
-                    const int cid = bid[(long long)jb.ctile * TC + e];
-                    float* o = r + (e >> 1) * (2 * REC) + (e & 1);
-                    if (cid >= 0) {
-#pragma unroll
-                        for (int c = 0; c < kMaxD; ++c) o[2 * c] = c < P.d ? P.xs[(size_t)cid * P.d + c] : 0.f;
-                        o[16] = P.err_coef * P.vn[cid]; o[18] = P.isp[cid]; o[20] = 2.4e-7f * P.xmax[cid];
-                        o[22] = __int_as_float(cid);
-                    } else {
-#pragma unroll
-                        for (int c = 0; c < 11; ++c) o[2 * c] = 0.f;
-                        o[22] = __int_as_float(-1);
-                    }
-                }
-                __syncwarp();
-                if (lane == 0) sm::mbar_arrive(&recf[acc]);
+                sm::mbar_arrive_expect_tx(&recf[acc], (unsigned)(TC * REC * sizeof(float)));
+                sm::bulk_g2s(recs + (size_t)acc * TC * REC, P.rec[jb.which & 1] + (size_t)jb.ctile * TC * REC,
+                             (unsigned)(TC * REC * sizeof(float)), &recf[acc]);
             }
         }
     } else {
@@ -481,6 +466,35 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
 }
 
 // -------------------------------------------------------------- operand prep
+// Candidate records of the sweep epilogue, in tile order (row r of a blocked operand
+// = row r here), built once per tree.  Rows 2i and 2i+1 of a tile share 2 * REC
+// floats with their fields interleaved (field f of row e at (e >> 1) * 2 * REC + 2f +
+// (e & 1)) so that the epilogue bounds both pairs with one packed f32x2 instruction
+// per step.  Fields: the scaled coordinates (padded to kMaxD), err_coef * |v|,
+// 1/sqrt(p), 2.4e-7 max|x| and the id's bits (-1 for padding rows).
+__global__ void build_records_kernel(const int* __restrict__ ids, long long rows, const float* __restrict__ xs, int d,
+                                     const float* __restrict__ vn, const float* __restrict__ isp,
+                                     const float* __restrict__ xmax, float err_coef, float* __restrict__ rec) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const long long tile = r / TC;
+    const int e = (int)(r - tile * TC);
+    float* o = rec + tile * (TC * REC) + (e >> 1) * (2 * REC) + (e & 1);
+    const int cid = ids[r];
+    if (cid >= 0) {
+#pragma unroll
+        for (int c = 0; c < kMaxD; ++c) o[2 * c] = c < d ? xs[(size_t)cid * d + c] : 0.f;
+        o[16] = err_coef * vn[cid];
+        o[18] = isp[cid];
+        o[20] = 2.4e-7f * xmax[cid];
+        o[22] = __int_as_float(cid);
+    } else {
+#pragma unroll
+        for (int c = 0; c < 11; ++c) o[2 * c] = 0.f;
+        o[22] = __int_as_float(-1);
+    }
+}
+
 // hi/lo split of V rows into the blocked layout.  rowmap[r] = dataset row of
 // blocked row r (or -1 for a zero row).  One thread per (row, 8-column group).
 __global__ void split_blocked_kernel(const float* __restrict__ v, int m, const int* __restrict__ rowmap,
@@ -969,6 +983,7 @@ struct State {
     long long* lvl_meta = nullptr;          // [nlevels][3]: size, row_off, rows_pad
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
     unsigned* isp_max = nullptr;            // bits of max 1/sqrt(p) over the dataset rows
+    float *rec_lvl = nullptr, *rec_ds = nullptr;  // sweep candidate records, tile order
     double* inv_ls64 = nullptr;
     float* inv_ls_df = nullptr;             // (hi, lo) float pairs of 1 / lengthscale
     int* status = nullptr;
@@ -1325,7 +1340,7 @@ void ct_tree::release_screen() {
     cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
     cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
-    cudaFree(S->inv_ls_df); cudaFree(S->isp_max);
+    cudaFree(S->inv_ls_df); cudaFree(S->isp_max); cudaFree(S->rec_ds); cudaFree(S->rec_lvl);
     cudaFree(S->bounds);
     if (S->slab_done) cudaEventDestroy(S->slab_done);
     delete S;
@@ -1368,6 +1383,8 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->isp, sizeof(float) * rows_q);
     A((void**)&S->xmax, sizeof(float) * rows_q);
     A((void**)&S->isp_max, sizeof(unsigned));
+    A((void**)&S->rec_ds, sizeof(float) * REC * S->rows_pad);
+    A((void**)&S->rec_lvl, sizeof(float) * REC * S->lvl_rows);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->inv_ls_df, sizeof(float) * 128);
     A((void**)&S->status, sizeof(int));
@@ -1409,6 +1426,11 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(S->lvl_meta, meta.data(), sizeof(long long) * meta.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->lvl_id, S->lvl_rows, S->lvl_hi, S->lvl_lo);
+        const float ec = err_coef_for(m);
+        build_records_kernel<<<grid_for(S->rows_pad), 256, 0, st>>>(S->b_id_ds, S->rows_pad, T->xs, T->d, S->vn,
+                                                                    S->isp, S->xmax, ec, S->rec_ds);
+        build_records_kernel<<<grid_for(S->lvl_rows), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs, T->d, S->vn,
+                                                                    S->isp, S->xmax, ec, S->rec_lvl);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -1691,6 +1713,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
     P.surv = surv; P.surv_cnt = surv_cnt; P.half_cap = half_cap; P.status = S->status;
     P.qtau = qtau; P.parts = parts;
+    P.rec[0] = S->rec_lvl; P.rec[1] = S->rec_ds;
     if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
     if (timing) cudaEventRecord(ev[3], st);
     // ---- rescoring (into the part lists when parts > 1)

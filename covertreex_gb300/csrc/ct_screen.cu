@@ -36,6 +36,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "ct_common.cuh"
@@ -104,6 +105,7 @@ struct MMAParams {
     int* surv; int* surv_cnt;
     int half_cap;        // survivor segment per (slot, column half)
     const float* rec[2]; // candidate records in tile order (levels, dataset), TC * REC floats per tile
+    const unsigned* xmax_max;  // bits of max |x_c| over the dataset rows
     int* status;
     unsigned* qtau;      // per query (slot / parts): the smallest part threshold, float bits
     int parts;           // candidate parts per query (slots s*parts .. s*parts+parts-1)
@@ -291,8 +293,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         unsigned gen = 0;  // query-tile generation, tags the shared row threshold
         float tau2 = 1.f;
         float nxq[kMaxD];  // negated query coordinates: x_c + (-x_q) is the rounded x_c - x_q
-        float vnq = 0.f, isq = 0.f, aq = 0.f;
+        float vnq = 0.f, isq = 0.f;
         int lim = 0;       // a candidate id is valid iff (unsigned)cid < (unsigned)lim
+        // Kernel-value error bound of the query, linear in d2 (see phase 1): for RBF the
+        // relative factor fk = alk d2 + bek, for Matern the d2 error ed2 = ale d2 + bee.
+        float alk = 0.f, bek = 0.f, ale = 0.f, bee = 0.f;
         // keep the pair iff (R + e) * isc >= thr_keep; it may enter the heap iff
         // (R - e) * isc > thr_heap (both derived from tau2 / the heap top; see below)
         float thr_keep = 0.f, thr_heap = 0.f;
@@ -311,11 +316,21 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 qid = slot >= 0 ? P.slot_id[slot] : -1;
                 hn = 0; cnt = 0; tau2 = 1.f; ++gen;
                 if (qid >= 0) {
-                    vnq = P.vn[qid]; isq = P.isp[qid]; aq = 2.4e-7f * P.xmax[qid];
+                    vnq = P.vn[qid]; isq = P.isp[qid];
 #pragma unroll
                     for (int c = 0; c < kMaxD; ++c) nxq[c] = c < P.d ? -P.xs[(size_t)qid * P.d + c] : 0.f;
                     // predecessor mode: 0 <= cid < qid; otherwise cid >= 0 (ids stay below INT_MAX)
                     lim = P.predecessor ? qid : 0x7fffffff;
+                    // Error of d2 from the scaled coordinates: (D+2) 2^-24 d2 from the sum plus
+                    // 2^-22 sum|dx| (|x_q| + |x_c|), sum|dx| <= sqrt(D d2) <= (D d2 + 1) / 2, with
+                    // |x_c| bounded by the dataset's largest: ed2 <= ale d2 + bee.  The RBF value's
+                    // relative error 6e-8 d2 + ed2 / 2 + 1e-6 <= alk d2 + bek.  The constants are
+                    // rounded up by 1e-5 relative, far above their own rounding.
+                    const float A = 2.4e-7f * (P.xmax[qid] + __uint_as_float(__ldg(P.xmax_max)));
+                    ale = (ced2 + 0.5f * A * dd) * 1.00001f;
+                    bee = 0.5f * A * 1.00001f;
+                    alk = (6e-8f + 0.5f * ced2 + 0.25f * A * dd) * 1.00001f;
+                    bek = (1e-6f + 0.25f * A) * 1.00001f;
                 }
                 thr_keep = 0.f;   // tau2 = 1: keep everything
                 thr_heap = -CT_FLT_MAX;  // heap not full: every pair enters
@@ -326,6 +341,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             const float* rb = recs + (size_t)acc * TC * REC;
             const bool keep_job = !(jb.which & 2);
             const bool feed_heap = !(jb.which & 4);
+            const bool fast_ids = (jb.which & 8) != 0;
             if (MODE == MODE_SWEEP && qid >= 0) {
                 // the other half's threshold, when it belongs to this query tile
                 const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
@@ -351,65 +367,66 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 if (qid < 0) continue;
                 // Phase 1, no stores: certified bounds of the group's 8 pairs, as
                 //   blo = (R - e) * isc (heap test)  and  bhi = (R + e) * isc (survivor test),
-                // +inf for the query itself, -inf for padding and predecessor-violating pairs.
-                // Free of stores, the pairs' loads and arithmetic overlap.
+                // +inf for the query itself, -inf for predecessor-violating pairs and NaN for
+                // padding rows (their 1/sqrt(p) is NaN, so every test fails).  Jobs flagged 8
+                // hold only candidate ids below every query id of the tile and skip the id
+                // tests.  Free of stores, the pairs' loads and arithmetic overlap.
                 float blo[8], bhi[8];
                 int bid[8];
+                auto phase1 = [&](auto check_ids) {
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    // columns col0 + 2i (.x) and col0 + 2i + 1 (.y)
-                    const float4* r4 = (const float4*)(rb + ((col0 >> 1) + i) * (2 * REC));
-                    const float4 m0 = r4[4];  // err_coef * |v_c|, 1/sqrt(p_c)
-                    const float4 m1 = r4[5];  // 2.4e-7 max|x_c|, id
-                    const float2 err = make_float2(m0.x, m0.y), isc = make_float2(m0.z, m0.w);
-                    float2 d2 = make_float2(0.f, 0.f), t;
+                    for (int i = 0; i < 4; ++i) {
+                        // columns col0 + 2i (.x) and col0 + 2i + 1 (.y)
+                        const float4* r4 = (const float4*)(rb + ((col0 >> 1) + i) * (2 * REC));
+                        const float4 m0 = r4[4];  // err_coef * |v_c|, 1/sqrt(p_c)
+                        const float4 m1 = r4[5];  // 2.4e-7 max|x_c| (unused), id
+                        const float2 err = make_float2(m0.x, m0.y), isc = make_float2(m0.z, m0.w);
+                        float2 d2 = make_float2(0.f, 0.f), t;
 #pragma unroll
-                    for (int h = 0; h < DP / 2; ++h) {
-                        const float4 x = r4[h];
-                        t = __fadd2_rn(make_float2(x.x, x.y), make_float2(nxq[2 * h], nxq[2 * h]));
-                        d2 = __ffma2_rn(t, t, d2);
-                        t = __fadd2_rn(make_float2(x.z, x.w), make_float2(nxq[2 * h + 1], nxq[2 * h + 1]));
-                        d2 = __ffma2_rn(t, t, d2);
+                        for (int h = 0; h < DP / 2; ++h) {
+                            const float4 x = r4[h];
+                            t = __fadd2_rn(make_float2(x.x, x.y), make_float2(nxq[2 * h], nxq[2 * h]));
+                            d2 = __ffma2_rn(t, t, d2);
+                            t = __fadd2_rn(make_float2(x.z, x.w), make_float2(nxq[2 * h + 1], nxq[2 * h + 1]));
+                            d2 = __ffma2_rn(t, t, d2);
+                        }
+                        float2 kv, ek;
+                        if (KT == 0) {
+                            const float2 h = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);
+                            kv = __fmul2_rn(make_float2(P.var, P.var), make_float2(__expf(h.x), __expf(h.y)));
+                            ek = __fmul2_rn(kv, __ffma2_rn(make_float2(alk, alk), d2, make_float2(bek, bek)));
+                        } else {
+                            const float2 ed2 = __ffma2_rn(make_float2(ale, ale), d2, make_float2(bee, bee));
+                            const float aa = 2.2360679775f * sqrtf(d2.x), ab = 2.2360679775f * sqrtf(d2.y);
+                            const float ea = __expf(-aa), eb = __expf(-ab);
+                            kv.x = P.var * (1.f + aa + aa * aa * 0.33333334f) * ea;
+                            kv.y = P.var * (1.f + ab + ab * ab * 0.33333334f) * eb;
+                            ek.x = kv.x * (1e-6f + 2.4e-7f * aa) + P.var * (0.8334f * ed2.x + 1e-7f * aa * aa) * (1.f + aa) * ea;
+                            ek.y = kv.y * (1e-6f + 2.4e-7f * ab) + P.var * (0.8334f * ed2.y + 1e-7f * ab * ab) * (1.f + ab) * eb;
+                        }
+                        const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
+                        const float2 R = make_float2(fabsf(dif.x), fabsf(dif.y));
+                        const float2 e = __fadd2_rn(__ffma2_rn(make_float2(vnq, vnq), err, ek),
+                                                    __ffma2_rn(R, make_float2(1.2e-7f, 1.2e-7f), make_float2(1e-30f, 1e-30f)));
+                        const float2 lo = __fmul2_rn(__fadd2_rn(R, make_float2(-e.x, -e.y)), isc);
+                        const float2 hi = __fmul2_rn(__fadd2_rn(R, e), isc);
+                        const int ca = __float_as_int(m1.z), cb = __float_as_int(m1.w);
+                        if constexpr (decltype(check_ids)::value) {
+                            const bool va = (unsigned)ca < (unsigned)lim, vb = (unsigned)cb < (unsigned)lim;
+                            const float inf = __int_as_float(0x7f800000);
+                            blo[2 * i] = !va ? -inf : (ca == qid ? inf : lo.x);
+                            bhi[2 * i] = !va ? -inf : (ca == qid ? inf : hi.x);
+                            blo[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : lo.y);
+                            bhi[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : hi.y);
+                        } else {
+                            blo[2 * i] = lo.x; bhi[2 * i] = hi.x;
+                            blo[2 * i + 1] = lo.y; bhi[2 * i + 1] = hi.y;
+                        }
+                        bid[2 * i] = ca;
+                        bid[2 * i + 1] = cb;
                     }
-                    // Certified error of the kernel value.  d2 error: (D+2) 2^-24 d2 from the
-                    // sum plus 2^-22 sum|dx| (|x_q| + |x_c|) from the scaled coordinates, with
-                    // sum|dx| <= sqrt(D d2) <= (D d2 + 1) / 2.
-                    const float2 axm = __fadd2_rn(make_float2(aq, aq), make_float2(m1.x, m1.y));
-                    const float2 u = __ffma2_rn(make_float2(dd, dd), d2, make_float2(1.f, 1.f));
-                    const float2 ed2 =
-                        __ffma2_rn(make_float2(ced2, ced2), d2, __fmul2_rn(__fmul2_rn(make_float2(0.5f, 0.5f), axm), u));
-                    float2 kv, ek;
-                    if (KT == 0) {
-                        const float2 h = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);
-                        kv = __fmul2_rn(make_float2(P.var, P.var), make_float2(__expf(h.x), __expf(h.y)));
-                        const float2 f = __ffma2_rn(make_float2(6e-8f, 6e-8f), d2,
-                                                    __ffma2_rn(make_float2(0.5f, 0.5f), ed2, make_float2(1e-6f, 1e-6f)));
-                        ek = __fmul2_rn(kv, f);
-                    } else {
-                        const float aa = 2.2360679775f * sqrtf(d2.x), ab = 2.2360679775f * sqrtf(d2.y);
-                        const float ea = __expf(-aa), eb = __expf(-ab);
-                        kv.x = P.var * (1.f + aa + aa * aa * 0.33333334f) * ea;
-                        kv.y = P.var * (1.f + ab + ab * ab * 0.33333334f) * eb;
-                        ek.x = kv.x * (1e-6f + 2.4e-7f * aa) + P.var * (0.8334f * ed2.x + 1e-7f * aa * aa) * (1.f + aa) * ea;
-                        ek.y = kv.y * (1e-6f + 2.4e-7f * ab) + P.var * (0.8334f * ed2.y + 1e-7f * ab * ab) * (1.f + ab) * eb;
-                    }
-                    const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
-                    const float2 R = make_float2(fabsf(dif.x), fabsf(dif.y));
-                    const float2 e = __fadd2_rn(__ffma2_rn(make_float2(vnq, vnq), err, ek),
-                                                __ffma2_rn(R, make_float2(1.2e-7f, 1.2e-7f), make_float2(1e-30f, 1e-30f)));
-                    const float2 lo = __fmul2_rn(__fadd2_rn(R, make_float2(-e.x, -e.y)), isc);
-                    const float2 hi = __fmul2_rn(__fadd2_rn(R, e), isc);
-                    // +inf for the query itself, -inf for padding and predecessor-violating pairs
-                    const int ca = __float_as_int(m1.z), cb = __float_as_int(m1.w);
-                    const bool va = (unsigned)ca < (unsigned)lim, vb = (unsigned)cb < (unsigned)lim;
-                    const float inf = __int_as_float(0x7f800000);
-                    blo[2 * i] = !va ? -inf : (ca == qid ? inf : lo.x);
-                    bhi[2 * i] = !va ? -inf : (ca == qid ? inf : hi.x);
-                    blo[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : lo.y);
-                    bhi[2 * i + 1] = !vb ? -inf : (cb == qid ? inf : hi.y);
-                    bid[2 * i] = ca;
-                    bid[2 * i + 1] = cb;
-                }
+                };
+                if (fast_ids) phase1(std::false_type{}); else phase1(std::true_type{});
                 // Phase 2: survivors and heap against the current thresholds.  Phase 1's
                 // values do not depend on the thresholds, so this keeps and heaps exactly
                 // the pairs that pair-by-pair processing would.  Most groups have no pair
@@ -471,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
 // floats with their fields interleaved (field f of row e at (e >> 1) * 2 * REC + 2f +
 // (e & 1)) so that the epilogue bounds both pairs with one packed f32x2 instruction
 // per step.  Fields: the scaled coordinates (padded to kMaxD), err_coef * |v|,
-// 1/sqrt(p), 2.4e-7 max|x| and the id's bits (-1 for padding rows).
+// 1/sqrt(p) (NaN for padding rows), 2.4e-7 max|x| and the id's bits (-1 for padding rows).
 __global__ void build_records_kernel(const int* __restrict__ ids, long long rows, const float* __restrict__ xs, int d,
                                      const float* __restrict__ vn, const float* __restrict__ isp,
                                      const float* __restrict__ xmax, float err_coef, float* __restrict__ rec) {
@@ -491,6 +508,7 @@ __global__ void build_records_kernel(const int* __restrict__ ids, long long rows
     } else {
 #pragma unroll
         for (int c = 0; c < 11; ++c) o[2 * c] = 0.f;
+        o[18] = __int_as_float(0x7fc00000);  // NaN 1/sqrt(p): every bound test of the row fails
         o[22] = __int_as_float(-1);
     }
 }
@@ -984,6 +1002,7 @@ struct State {
     float *vn = nullptr, *isp = nullptr, *xmax = nullptr;
     unsigned* isp_max = nullptr;            // bits of max 1/sqrt(p) over the dataset rows
     float *rec_lvl = nullptr, *rec_ds = nullptr;  // sweep candidate records, tile order
+    unsigned* xmax_max = nullptr;                 // bits of max |x| over the dataset rows
     double* inv_ls64 = nullptr;
     float* inv_ls_df = nullptr;             // (hi, lo) float pairs of 1 / lengthscale
     int* status = nullptr;
@@ -1022,6 +1041,10 @@ struct JobUnit {
     int lo_tile;          // dataset tiles from lo_tile follow the level tiles
     int warm, count;      // warm-up jobs; all jobs
     long long off;        // first job in the flat list
+    // Jobs whose candidate ids all lie below every query id of the tile need no
+    // predecessor or self test (flag 8): level tiles when the level size is at most
+    // the tile's smallest query id, dataset tiles below ds_fast_end.
+    int fast_lvl, ds_fast_end;
 };
 
 // w-th tile of the spiral cc, cc+1, cc-1, cc+2, cc-2, ... clipped to [t0, t0 + ntl)
@@ -1102,10 +1125,10 @@ __global__ void gen_jobs_kernel(const JobUnit* __restrict__ units, Job* __restri
         int which, ctile;
         if (w < U.ntl) {
             ctile = spiral_tile(U, w);
-            which = warmup ? 2 : (j < U.warm ? 4 : 0);
+            which = (warmup ? 2 : (j < U.warm ? 4 : 0)) | (U.fast_lvl ? 8 : 0);
         } else {
             ctile = U.lo_tile + (w - U.ntl);
-            which = 1;
+            which = 1 | (ctile < U.ds_fast_end ? 8 : 0);
         }
         jobs[U.off + i] = Job{U.qx, ctile, which, i == 0 ? 1 : 0};
     }
@@ -1340,7 +1363,7 @@ void ct_tree::release_screen() {
     cudaFree(S->hil_order); cudaFree(S->hil_key); cudaFree(S->ds_hi); cudaFree(S->ds_lo); cudaFree(S->b_id_ds);
     cudaFree(S->lvl_hi); cudaFree(S->lvl_lo); cudaFree(S->lvl_id); cudaFree(S->lvl_key); cudaFree(S->lvl_meta);
     cudaFree(S->vn); cudaFree(S->isp); cudaFree(S->xmax); cudaFree(S->inv_ls64); cudaFree(S->status);
-    cudaFree(S->inv_ls_df); cudaFree(S->isp_max); cudaFree(S->rec_ds); cudaFree(S->rec_lvl);
+    cudaFree(S->inv_ls_df); cudaFree(S->isp_max); cudaFree(S->rec_ds); cudaFree(S->rec_lvl); cudaFree(S->xmax_max);
     cudaFree(S->bounds);
     if (S->slab_done) cudaEventDestroy(S->slab_done);
     delete S;
@@ -1383,6 +1406,7 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->isp, sizeof(float) * rows_q);
     A((void**)&S->xmax, sizeof(float) * rows_q);
     A((void**)&S->isp_max, sizeof(unsigned));
+    A((void**)&S->xmax_max, sizeof(unsigned));
     A((void**)&S->rec_ds, sizeof(float) * REC * S->rows_pad);
     A((void**)&S->rec_lvl, sizeof(float) * REC * S->lvl_rows);
     A((void**)&S->inv_ls64, sizeof(double) * 64);
@@ -1402,7 +1426,9 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
         split_blocked_kernel<<<152 * 8, 256, 0, st>>>(T->vnat, m, S->b_id_ds, S->rows_pad, S->ds_hi, S->ds_lo);
         point_scalars_kernel<<<grid_for(n), 256, 0, st>>>(T->vnat, T->p, T->xs, n, m, T->d, S->vn, S->isp, S->xmax);
         e = cudaMemsetAsync(S->isp_max, 0, sizeof(unsigned), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(S->xmax_max, 0, sizeof(unsigned), st);
         if (e == cudaSuccess) max_bits_kernel<<<grid_for(n), 256, 0, st>>>(S->isp, n, S->isp_max);
+        if (e == cudaSuccess) max_bits_kernel<<<grid_for(n), 256, 0, st>>>(S->xmax, n, S->xmax_max);
         if (e == cudaSuccess) e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(order_h.data(), S->hil_order, sizeof(int) * n, cudaMemcpyDeviceToHost, st);
@@ -1544,13 +1570,17 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     // dataset tiles [lo_tile, hi_tile) that hold ids beyond the level.
     struct TileSpec {
         int cc, t0, ntl, lo_tile, hi_tile;
+        long long lvl_size, min_q;  // the spiral level's size; the tile's smallest query id
     };
-    std::vector<TileSpec> spec(nqt, TileSpec{0, 0, 0, 0, 0});
+    std::vector<TileSpec> spec(nqt, TileSpec{0, 0, 0, 0, 0, 0, 0});
     std::vector<char> busy(nqt, 0);
     const long long n_ds_tiles = S->rows_pad / TC;
     for (long long t = 0; t < nqt; ++t) {
-        long long maxq = -1;
-        for (long long r = t * TQ; r < (t + 1) * TQ; ++r) maxq = std::max<long long>(maxq, hrow_id[r]);
+        long long maxq = -1, minq = LLONG_MAX;
+        for (long long r = t * TQ; r < (t + 1) * TQ; ++r) {
+            maxq = std::max<long long>(maxq, hrow_id[r]);
+            if (hrow_id[r] >= 0) minq = std::min<long long>(minq, hrow_id[r]);
+        }
         if (maxq < 0) continue;  // no valid query in this tile
         long long r = std::min<long long>(t * TQ + TQ / 2, nq - 1);
         auto row_of = [&](long long rr) -> long long {
@@ -1565,11 +1595,13 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             for (int l = 0; l < nlev; ++l)
                 if (row >= S->levels[l].row_off && row < S->levels[l].row_off + S->levels[l].rows_pad) li = l;
         TileSpec& sp = spec[t];
+        sp.min_q = minq;
         if (li >= 0) {
             const Level& L = S->levels[li];
             sp.t0 = (int)(L.row_off / TC);
             sp.ntl = (int)(L.rows_pad / TC);
             sp.cc = (int)std::min<long long>(std::max<long long>(row / TC, sp.t0), sp.t0 + sp.ntl - 1);
+            sp.lvl_size = L.size;
         }
         if (predecessor) {
             // ids >= the level size are not in the level: sweep them in dataset order
@@ -1624,6 +1656,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             u.qx = (int)(t * parts + pp); u.p = pp; u.parts = parts;
             u.cc = sp.cc; u.t0 = sp.t0; u.ntl = sp.ntl; u.lo_tile = sp.lo_tile;
             u.warm = warm; u.count = warm + mine; u.off = 0;
+            u.fast_lvl = (sp.ntl > 0 && sp.lvl_size <= sp.min_q) ? 1 : 0;
+            u.ds_fast_end = (int)std::min<long long>(sp.min_q / TC, (long long)INT_MAX);
             units.push_back(u);
         }
     }
@@ -1713,7 +1747,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
     P.surv = surv; P.surv_cnt = surv_cnt; P.half_cap = half_cap; P.status = S->status;
     P.qtau = qtau; P.parts = parts;
-    P.rec[0] = S->rec_lvl; P.rec[1] = S->rec_ds;
+    P.rec[0] = S->rec_lvl; P.rec[1] = S->rec_ds; P.xmax_max = S->xmax_max;
     if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
     if (timing) cudaEventRecord(ev[3], st);
     // ---- rescoring (into the part lists when parts > 1)

@@ -79,6 +79,7 @@ class CtStats(ctypes.Structure):
         ("rescore_ms", ctypes.c_double),
         ("screen_pairs_main", ctypes.c_int64),
         ("overflow_queries", ctypes.c_int64),
+        ("pairs_exhaustive", ctypes.c_int64),
     ]
 
     def as_dict(self):

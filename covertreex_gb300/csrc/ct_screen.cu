@@ -63,8 +63,9 @@ constexpr int kThreads = 96 + kEpiThreads;  // producer, MMA issuer, staging, ep
 constexpr int kMaxD = 8;
 constexpr int kMaxK = 64;                   // heap capacity per epilogue thread
 constexpr int REC = 12;                     // floats per staged candidate record
-constexpr int kSurvCap = 1024;  // default survivors per query slot (two column halves)
+constexpr int kSurvCap = 1024;  // survivors per query slot (two column halves), at most RBUF
 constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
+static_assert(kSurvCap <= RBUF, "a slot's survivors must fit the rescoring buffer");
 
 enum Mode { MODE_DEBUG = 0, MODE_SWEEP = 1 };
 
@@ -605,6 +606,13 @@ struct RescoreParams {
     // each followed by its candidate parts, so neighbouring warps gather overlapping rows
     const int* order; int parts;
     int chunk;  // candidates per item of the exhaustive pass (parts == 1)
+    // certified FP32 filter of the survivor pass (see rescore_kernel)
+    const float* xs;             // scaled coordinates x / l (f32, as the sweep uses them)
+    const float* vn;             // |v| rounded up
+    const float* isp;            // 1 / sqrt(p)
+    const float* xmax;           // max |x / l| per row
+    const unsigned* xmax_max;    // bits of the dataset's largest xmax
+    const unsigned* isp_max;     // bits of the dataset's largest 1 / sqrt(p)
 };
 
 // ---------------------------------------------------------- double-float
@@ -800,46 +808,187 @@ __device__ __forceinline__ float exact_from_dot(const RescoreParams& P, int q, i
 __device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& fill, int k, bool has,
                                                  unsigned long long key);
 
-// One warp per query slot.  Candidates: the survivor list, or the full range
-// [0, limit) for slots listed in full_slots.  Streaming top-k through a sorted
-// shared buffer: entries [0, k) hold the current best, new candidates fill the
-// rest, and a full buffer is re-sorted.
-__global__ void rescore_kernel(RescoreParams P, int use_full) {
+// Plain FP32 dots of the query slice with NC candidate rows (the split of warp_dots,
+// one FMA per element, then a butterfly sum).  Each lane's chain has m/32 roundings
+// and the butterfly 5 more, so |error| <= (m/32 + 7) 2^-24 |v_q| |v_c|.
+template <int NC>
+__device__ __forceinline__ void warp_dots_f32(const float* __restrict__ V, int m, const int (&cid)[NC],
+                                              const float (&vq)[32], float (&out)[NC]) {
+    const int lane = threadIdx.x & 31;
+    const int per = m >> 5;
+    float s[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) s[c] = 0.f;
+    if ((per & 3) == 0) {
+#pragma unroll
+        for (int t4 = 0; t4 < 8; ++t4) {
+            if (t4 * 4 < per) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const float4 x = cid[c] >= 0 ? __ldg((const float4*)(V + (size_t)cid[c] * m + (size_t)lane * per) + t4)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+                    s[c] = __fmaf_rn(vq[4 * t4 + 0], x.x, s[c]);
+                    s[c] = __fmaf_rn(vq[4 * t4 + 1], x.y, s[c]);
+                    s[c] = __fmaf_rn(vq[4 * t4 + 2], x.z, s[c]);
+                    s[c] = __fmaf_rn(vq[4 * t4 + 3], x.w, s[c]);
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int t = 0; t < 32; ++t) {
+            if (t < per) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const float b = cid[c] >= 0 ? __ldg(V + (size_t)cid[c] * m + (size_t)lane * per + t) : 0.f;
+                    s[c] = __fmaf_rn(vq[t], b, s[c]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s[c] = __fadd_rn(s[c], __shfl_xor_sync(0xffffffffu, s[c], off));
+        out[c] = s[c];
+    }
+}
+
+// Certified bounds [dl2, du2] of d^2 = 1 - |rho| for one pair from an FP32 dot with
+// error <= ed: the kernel value from the scaled f32 coordinates with the sweep's error
+// model (ale, bee, alk, bek as there), the normalisation 1 / sqrt(max(p_q p_c, 1e-18)).
+__device__ __forceinline__ void pair_bounds_f32(const RescoreParams& P, int q, int c, float dot, float ed, float isq,
+                                                float alk, float bek, float ale, float bee, float& dl2, float& du2) {
+    float d2 = 0.f;
+    for (int a = 0; a < P.d; ++a) {
+        const float t = __fsub_rn(P.xs[(size_t)c * P.d + a], P.xs[(size_t)q * P.d + a]);
+        d2 = __fmaf_rn(t, t, d2);
+    }
+    float kv, ek;
+    if (P.kernel_type == 0) {
+        kv = __fmul_rn(P.var, __expf(__fmul_rn(-0.5f, d2)));
+        ek = __fmul_rn(kv, __fmaf_rn(alk, d2, bek));
+    } else {
+        const float ed2 = __fmaf_rn(ale, d2, bee);
+        const float a = 2.2360679775f * sqrtf(d2);
+        const float ea = __expf(-a);
+        kv = P.var * (1.f + a + a * a * 0.33333334f) * ea;
+        ek = kv * (1e-6f + 2.4e-7f * a) + P.var * (0.8334f * ed2 + 1e-7f * a * a) * (1.f + a) * ea;
+    }
+    const float R = fabsf(__fsub_rn(kv, dot));
+    const float e = __fadd_rn(__fadd_rn(ed, ek), __fmaf_rn(R, 1.2e-7f, 1e-30f));
+    const float sc = fminf(__fmul_rn(isq, P.isp[c]), 1e9f);
+    const float rl = __fmul_rn(__fmul_rn(fmaxf(__fsub_rn(R, e), 0.f), sc), 1.f - 2e-6f);
+    const float rh = __fmul_rn(__fmul_rn(__fadd_rn(R, e), sc), 1.f + 2e-6f);
+    du2 = 1.f - fminf(rl, 1.f);
+    dl2 = fmaxf(1.f - fminf(rh, 1.f), 0.f);
+}
+
+// Survivor rescoring, one warp per query slot, in two steps.
+//  F: every survivor gets certified bounds [dl2, du2] of its d^2 from a plain FP32 dot
+//     (error (m/32 + 7) 2^-24 |v_q| |v_c|, some fifty times tighter than the sweep's
+//     BF16 bound) at one instruction per element.  tau = the k-th smallest du2, widened
+//     by the double-float error of the exact distances, bounds the k-th distance.
+//  E: only survivors with dl2 <= tau are rescored exactly (compensated FP32 dot,
+//     double-float distance); the others cannot enter the top k.
+// Streaming top-k of E through a sorted shared buffer: entries [0, k) hold the current
+// best, new candidates fill the rest, and a full buffer is re-sorted.  Shared memory per
+// warp: RBUF keys, then RBUF floats (du2, reused for the kept ids).
+__global__ void rescore_kernel(RescoreParams P) {
     extern __shared__ unsigned long long rkeys_all[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x / 32;
     unsigned long long* keys = rkeys_all + (size_t)warp * RBUF;
-    long long w = (long long)blockIdx.x * wpb + warp;
-    long long nwork = use_full ? P.nfull : P.nslots;
-    if (w >= nwork) return;
-    const int slot = use_full ? P.full_slots[w]
-                              : (P.order ? P.order[w / P.parts] * P.parts + (int)(w % P.parts) : (int)w);
-    const int c0 = use_full ? 0 : P.surv_cnt[2 * slot];
-    const int c1 = use_full ? 0 : P.surv_cnt[2 * slot + 1];
-    if (!use_full && (c0 > P.half_cap || c1 > P.half_cap)) return;  // handled by the exhaustive pass
+    float* du2s = (float*)(rkeys_all + (size_t)wpb * RBUF) + (size_t)warp * RBUF;
+    int* kept = (int*)du2s;
+    const long long w = (long long)blockIdx.x * wpb + warp;
+    if (w >= P.nslots) return;
+    const int slot = P.order ? P.order[w / P.parts] * P.parts + (int)(w % P.parts) : (int)w;
+    const int c0 = P.surv_cnt[2 * slot];
+    const int c1 = P.surv_cnt[2 * slot + 1];
+    if (c0 > P.half_cap || c1 > P.half_cap) return;  // handled by the exhaustive pass
     const int q = P.slot_id[slot];
     if (q < 0) {
         for (int j = lane; j < P.k; j += 32) { P.out_idx[(size_t)slot * P.k + j] = -1; P.out_dist[(size_t)slot * P.k + j] = CT_FLT_MAX; }
         return;
     }
     const int k = P.k;
+    const int count = c0 + c1;  // <= 2 half_cap <= RBUF
     float vql[32];
     load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
+    // per-query constants of the bounds
+    const float isq = P.isp[q];
+    const float ed_q = (float)((P.m >> 5) + 7) * 5.97e-8f * P.vn[q];
+    const float dd = (float)P.d, ced2 = (dd + 2.f) * 5.97e-8f;
+    const float A = 2.4e-7f * (P.xmax[q] + __uint_as_float(__ldg(P.xmax_max)));
+    const float ale = (ced2 + 0.5f * A * dd) * 1.00001f, bee = 0.5f * A * 1.00001f;
+    const float alk = (6e-8f + 0.5f * ced2 + 0.25f * A * dd) * 1.00001f, bek = (1e-6f + 0.25f * A) * 1.00001f;
+    // ---- F: certified FP32 bounds of every survivor
+    for (int base = 0; base < count; base += 32) {
+        const int ci = base + lane;
+        const int cid = ci < count ? (ci < c0 ? P.surv[(size_t)(2 * slot) * P.half_cap + ci]
+                                              : P.surv[(size_t)(2 * slot + 1) * P.half_cap + (ci - c0)])
+                                   : -1;
+        const int nb = count - base < 32 ? count - base : 32;
+        float mydot = 0.f;
+        for (int t = 0; t < nb; t += 4) {
+            int cc[4];
+            float dots[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int src = __shfl_sync(0xffffffffu, cid, (t + u) & 31);
+                cc[u] = (t + u) < nb ? src : -1;
+            }
+            warp_dots_f32<4>(P.v, P.m, cc, vql, dots);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (lane == t + u) mydot = dots[u];
+        }
+        if (ci < count) {
+            float dl2 = 0.f, du2 = 0.f;  // the query itself: d = 0
+            if (cid != q)
+                pair_bounds_f32(P, q, cid, mydot, __fmul_rn(ed_q, P.vn[cid]), isq, alk, bek, ale, bee, dl2, du2);
+            keys[ci] = ((unsigned long long)__float_as_uint(dl2) << 32) | (unsigned)cid;
+            du2s[ci] = du2;
+        }
+    }
+    __syncwarp();
+    // tau: the k-th smallest du2 (bisection over the bit patterns of these non-negative
+    // floats), plus the margin of the seeded thresholds; every survivor when fewer than k
+    float tau = CT_FLT_MAX;
+    if (count > k) {
+        unsigned lo = 0, hi = 0x3f800000u;  // du2 <= 1
+        while (lo < hi) {
+            const unsigned mid = lo + ((hi - lo) >> 1);
+            int c = 0;
+            for (int i = lane; i < count; i += 32) c += __float_as_uint(du2s[i]) <= mid;
+            c = __reduce_add_sync(0xffffffffu, c);
+            if (c >= k) hi = mid; else lo = mid + 1;
+        }
+        const float margin = 4e-12f * fminf(isq * __uint_as_float(__ldg(P.isp_max)) * 1.01f, 1e9f) + 1e-12f;
+        tau = __fadd_ru(__fmul_ru(__uint_as_float(lo), 1.000004f), margin);
+    }
+    __syncwarp();
+    // compaction of the survivors that can still be among the k nearest
+    int nk = 0;
+    for (int base = 0; base < count; base += 32) {
+        const int ci = base + lane;
+        unsigned long long key = ci < count ? keys[ci] : 0ULL;
+        const bool keep = ci < count && __uint_as_float((unsigned)(key >> 32)) <= tau;
+        const unsigned mask = __ballot_sync(0xffffffffu, keep);
+        __syncwarp();  // every lane has read its key before the ids overwrite du2s
+        if (keep) kept[nk + __popc(mask & ((1u << lane) - 1u))] = (int)(unsigned)(key & 0xffffffffULL);
+        nk += __popc(mask);
+    }
     for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
     __syncwarp();
-    long long count = use_full ? (P.predecessor ? (long long)q : P.n) : (long long)(c0 + c1);
+    // ---- E: exact rescoring of the kept survivors
     int fill = k;  // next free position in the buffer
-    long long evals = 0;
-    for (long long base = 0; base < count; base += 32) {
-        // each lane fetches one candidate id; the warp scores them four at a time
-        long long ci = base + lane;
-        int cid = -1;
-        if (ci < count)
-            cid = use_full ? (int)ci
-                           : (ci < c0 ? P.surv[(size_t)(2 * slot) * P.half_cap + ci]
-                                      : P.surv[(size_t)(2 * slot + 1) * P.half_cap + (ci - c0)]);
+    for (int base = 0; base < nk; base += 32) {
+        const int ci = base + lane;
+        const int cid = ci < nk ? kept[ci] : -1;
         df mydot = df{0.f, 0.f};
-        const int nb = (int)((count - base) < 32 ? (count - base) : 32);
+        const int nb = nk - base < 32 ? nk - base : 32;
         for (int t = 0; t < nb; t += 4) {
             int cc[4];
             df dots[4];
@@ -853,9 +1002,8 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
             for (int u = 0; u < 4; ++u)
                 if (lane == t + u) mydot = dots[u];
         }
-        float mydist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
-        evals += nb;
-        warp_topk_append(keys, fill, k, ci < count, pack_key(mydist, cid));
+        const float mydist = ci < nk ? exact_from_dot(P, q, cid, mydot) : 0.f;
+        warp_topk_append(keys, fill, k, ci < nk, pack_key(mydist, cid));
     }
     warp_bitonic_sort(keys, sort_len(fill));
     for (int j = lane; j < k; j += 32) {
@@ -864,7 +1012,7 @@ __global__ void rescore_kernel(RescoreParams P, int use_full) {
         P.out_idx[(size_t)slot * k + j] = ok ? (long long)(unsigned)(key & 0xffffffffULL) : -1LL;
         P.out_dist[(size_t)slot * k + j] = ok ? __uint_as_float((unsigned)(key >> 32)) : CT_FLT_MAX;
     }
-    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
+    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)nk);
 }
 
 // Exhaustive rescoring of overflowed queries, split for parallelism: each warp
@@ -1628,13 +1776,13 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         parts = (int)std::max<long long>(1, std::min<long long>(parts, max_jobs / 8));
     }
     const long long nslots = nq * parts;
-    // Survivor lists per slot: kSurvCap by default (CT_SCREEN_SURVIVOR_CAP overrides it,
-    // within 8 GiB for the call); a slot that overflows is rescored exhaustively.
+    // Survivor lists per slot: kSurvCap by default, at most RBUF (the survivor pass holds a
+    // slot's survivors in shared memory); CT_SCREEN_SURVIVOR_CAP lowers it.  A slot that
+    // overflows is rescored exhaustively.
     int half_cap = kSurvCap / 2;
     if (const char* env = std::getenv("CT_SCREEN_SURVIVOR_CAP")) {
         const long long want = std::atoll(env) / 2;
-        const long long fit = (8LL << 30) / (8LL * std::max<long long>(nslots, 1));
-        half_cap = (int)std::max<long long>(64, std::min<long long>({want, fit, 1LL << 20}));
+        half_cap = (int)std::max<long long>(32, std::min<long long>(want, RBUF / 2));
     }
     const long long rows_x = rows_q * parts;
     // Units (query tile, part): a heap-only warm-up over the part's first level tiles,
@@ -1759,18 +1907,21 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     R.nfull = 0; R.chunk = 4096;
     R.k = k; R.evals = evals_d;
     R.order = val_lvl; R.parts = parts;
+    R.xs = xs; R.vn = S->vn; R.isp = S->isp; R.xmax = S->xmax; R.xmax_max = S->xmax_max; R.isp_max = S->isp_max;
     R.out_idx = parts > 1 ? part_idx : (long long*)out_idx;
     R.out_dist = parts > 1 ? part_dist : out_dist;
     const int rwpb = 8;
     const size_t rsmem = sizeof(unsigned long long) * RBUF * rwpb;
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+    const size_t ssmem = (sizeof(unsigned long long) + sizeof(float)) * RBUF * rwpb;  // survivor pass
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem);
     if (e == cudaSuccess) {
-        rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, 0);
+        rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, ssmem, st>>>(R);
         collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, half_cap, full_list, nfull_d);
         e = cudaGetLastError();
         launches += 2;
     }
     int nfull = 0, status = 0;
+    long long exh_pairs = 0;  // candidates of the exhaustive pass (part tiles count whole tiles)
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nfull, nfull_d, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, S->status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -1812,6 +1963,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
                 if (fu[i] >= 0) total_tiles += flat_units[fu[i]].count - flat_units[fu[i]].warm;
             }
             tpc = (int)std::min<long long>(16, std::max<long long>(1, (total_tiles + target_items - 1) / target_items));
+            exh_pairs = total_tiles * TC;
             for (int i = 0; i < nfull; ++i) {
                 ibeg[i] = (int)pitems.size();
                 if (fu[i] < 0) continue;
@@ -1823,6 +1975,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         } else {
             long long total = 0;
             for (int i = 0; i < nfull; ++i) total += predecessor ? (long long)sid[fl[i]] : n;
+            exh_pairs = total;
             R.chunk = (int)std::min<long long>(4096, std::max<long long>(256, ((total + target_items - 1) / target_items + 255) / 256 * 256));
             for (int i = 0; i < nfull; ++i) {
                 ibeg[i] = (int)items.size();
@@ -1920,6 +2073,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
         stats->rescore_ms = ms_r;
         stats->screen_pairs_main = pairs_main;
         stats->overflow_queries = nfull;
+        stats->pairs_exhaustive = exh_pairs;
     }
     return CT_OK;
 }

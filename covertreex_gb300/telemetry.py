@@ -34,7 +34,8 @@ def query_telemetry(stats: Mapping[str, Any], form: str = "") -> dict:
         "subtrees_pruned": 0,
         "gpu": {"form": form, **{k: stats[k] for k in ("pairs_screened", "pairs_rescored", "kernel_launches",
                                                       "device_ms", "screen_ms", "threshold_ms", "rescore_ms",
-                                                      "screen_pairs_main", "overflow_queries") if k in stats}},
+                                                      "screen_pairs_main", "overflow_queries", "pairs_exhaustive")
+                                   if k in stats}},
     }
 
 

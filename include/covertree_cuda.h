@@ -71,14 +71,15 @@ typedef struct ct_tree ct_tree;
 typedef struct {
     int64_t distance_evals;   /* residual distances evaluated exactly (reference `distance_evals`) */
     int64_t pairs_screened;   /* query x candidate pairs screened by the BF16 passes          */
-    int64_t pairs_rescored;   /* pairs rescored in compensated FP32 + FP64                    */
+    int64_t pairs_rescored;   /* pairs rescored exactly (compensated FP32 dot, double-float distance) */
     int64_t kernel_launches;  /* engine kernels launched by the call                          */
     double device_ms;         /* device time of the whole call (timing enabled, else 0)       */
-    double screen_ms;         /* tensor-core screening kernel of the main sweep (Pass B)      */
-    double threshold_ms;      /* threshold pass (Pass A + k-th bound selection)               */
+    double screen_ms;         /* tensor-core screening sweep                                  */
+    double threshold_ms;      /* setup before the sweep: query order, seeded thresholds, jobs  */
     double rescore_ms;        /* rescoring kernels                                            */
     int64_t screen_pairs_main;/* pairs screened by the main sweep                             */
-    int64_t overflow_queries; /* queries whose survivor list overflowed (rescored exhaustively) */
+    int64_t overflow_queries; /* query slots whose survivor list overflowed (rescored exhaustively) */
+    int64_t pairs_exhaustive; /* of pairs_rescored, those of the exhaustive pass over overflowed slots */
 } ct_stats;
 
 /* Library version (major*10000 + minor*100 + patch). */

@@ -291,6 +291,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         float* heap = heaps + et;
         int lt = 0;
         int slot = -1, qid = -1, hn = 0, cnt = 0;
+        // A (row, half) whose survivor list overflowed is rescored exhaustively: it stops
+        // keeping and heaping (thresholds +inf), so that a tiny-p row, whose wide bounds
+        // pass nearly every pair, does not hold its warp in phase 2 for the rest of the sweep.
+        bool ovf = false;
         unsigned gen = 0;  // query-tile generation, tags the shared row threshold
         float tau2 = 1.f;
         float nxq[kMaxD];  // negated query coordinates: x_c + (-x_q) is the rounded x_c - x_q
@@ -315,7 +319,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 const long long arow = (long long)jb.qtile * TQ + row;
                 slot = P.a_slot[arow];
                 qid = slot >= 0 ? P.slot_id[slot] : -1;
-                hn = 0; cnt = 0; tau2 = 1.f; ++gen;
+                hn = 0; cnt = 0; tau2 = 1.f; ++gen; ovf = false;
                 if (qid >= 0) {
                     vnq = P.vn[qid]; isq = P.isp[qid];
 #pragma unroll
@@ -343,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             const bool keep_job = !(jb.which & 2);
             const bool feed_heap = !(jb.which & 4);
             const bool fast_ids = (jb.which & 8) != 0;
-            if (MODE == MODE_SWEEP && qid >= 0) {
+            if (MODE == MODE_SWEEP && qid >= 0 && !ovf) {
                 // the other half's threshold, when it belongs to this query tile
                 const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
                 if ((unsigned)(w >> 32) == gen) {
@@ -441,7 +445,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 for (int i = 0; i < 8; ++i) {
                     if (keep_job && bhi[i] >= thr_keep) {
                         if (cnt < P.half_cap) P.surv[((size_t)slot * 2 + half) * P.half_cap + cnt] = bid[i];
-                        ++cnt;
+                        if (++cnt > P.half_cap) {
+                            ovf = true;
+                            thr_keep = __int_as_float(0x7f800000);
+                            thr_heap = __int_as_float(0x7f800000);
+                        }
                     }
                     if (feed_heap && blo[i] > thr_heap) {
                         // exact certified upper bound of d^2 for this pair (0 for the query itself)

@@ -304,7 +304,9 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         // relative factor fk = alk d2 + bek, for Matern the d2 error ed2 = ale d2 + bee.
         float alk = 0.f, bek = 0.f, ale = 0.f, bee = 0.f;
         // keep the pair iff (R + e) * isc >= thr_keep; it may enter the heap iff
-        // (R - e) * isc > thr_heap (both derived from tau2 / the heap top; see below)
+        // (R - e) * isc > thr_heap, i.e. its d^2 upper bound is below tau2 (both derived
+        // from tau2: a pair at or above the row's threshold cannot lower it, since the
+        // half's k-th bound could only fall to tau2)
         float thr_keep = 0.f, thr_heap = 0.f;
 #pragma unroll
         for (int c = 0; c < kMaxD; ++c) nxq[c] = 0.f;
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     bek = (1e-6f + 0.25f * A) * 1.00001f;
                 }
                 thr_keep = 0.f;   // tau2 = 1: keep everything
-                thr_heap = -CT_FLT_MAX;  // heap not full: every pair enters
+                thr_heap = 0.f;   // and heap every pair whose |rho| bound is positive
             }
             if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) break;
             if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) break;
@@ -352,12 +354,20 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 const unsigned long long w = *(volatile unsigned long long*)&rowtau[row];
                 if ((unsigned)(w >> 32) == gen) {
                     const float t = __uint_as_float(~(unsigned)w);
-                    if (t < tau2) { tau2 = t; thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq; }
+                    if (t < tau2) {
+                        tau2 = t;
+                        thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq;
+                        thr_heap = (1.f - tau2) * (1.f + 2e-6f) / isq;
+                    }
                 }
                 // the other parts' thresholds of this query (any part's k-th upper
                 // bound bounds the query's k-th distance)
                 const float tg = __uint_as_float(__ldcg(&P.qtau[slot / P.parts]));
-                if (tg < tau2) { tau2 = tg; thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq; }
+                if (tg < tau2) {
+                    tau2 = tg;
+                    thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq;
+                    thr_heap = (1.f - tau2) * (1.f + 2e-6f) / isq;
+                }
             }
             for (int cc = 0; cc < 16; ++cc) {
                 float v[8];
@@ -465,10 +475,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                         }
                         if (changed) {
                             const float top = heap[0];
-                            thr_heap = (1.f - top) * (1.f + 2e-6f) / isq;
                             if (top < tau2) {
                                 tau2 = top;
                                 thr_keep = (1.f - tau2) * (1.f - 2e-6f) / isq;
+                                thr_heap = (1.f - tau2) * (1.f + 2e-6f) / isq;
                                 atomicMax(&rowtau[row], ((unsigned long long)gen << 32) |
                                                             (unsigned long long)(~__float_as_uint(tau2)));
                                 if (P.parts > 1) atomicMin(&P.qtau[slot / P.parts], __float_as_uint(tau2));

@@ -446,10 +446,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 // values do not depend on the thresholds, so this keeps and heaps exactly
                 // the pairs that pair-by-pair processing would.  Most groups have no pair
                 // to keep or heap; one test skips them (the thresholds then stay as they are).
-                bool any = false;
+                // (the group's largest bounds decide: fmaxf skips the NaN of padding rows)
+                float mh = bhi[0], ml = blo[0];
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    any |= (keep_job & (bhi[i] >= thr_keep)) | (feed_heap & (blo[i] > thr_heap));
+                for (int i = 1; i < 8; ++i) { mh = fmaxf(mh, bhi[i]); ml = fmaxf(ml, blo[i]); }
+                const bool any = (keep_job & (mh >= thr_keep)) | (feed_heap & (ml > thr_heap));
                 if (!any) continue;
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {

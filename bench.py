@@ -472,12 +472,12 @@ def main():
     achieved = alg_flops / (screen_ms / 1e3) / 1e12
     # DRAM bytes per screened pair of the sweep, from the ncu capture at N=65536 of the
     # same workload (profiles/screen_sweep_precision_workload.md), scaled to this launch
-    sweep_dram_bytes_per_pair = 7.02
+    sweep_dram_bytes_per_pair = 7.19
     roofline = {
         "bound": "tensor", "kernel": "screen_sweep_kernel (main sweep)", "achieved": achieved,
         "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
         "traffic": sweep_dram_bytes_per_pair * pairs_main,
-        "traffic_note": "bytes per launch: 7.02 B per screened pair (ncu, N=65536) x pairs of this launch",
+        "traffic_note": "bytes per launch: 7.19 B per screened pair (ncu, N=65536) x pairs of this launch",
         "peak_kind": f"bf16_tflops_sustained ({peak_kind})",
         "tensor_issued_tflops": issued_flops / (screen_ms / 1e3) / 1e12,
         "kernel_ms": screen_ms, "pairs_per_launch": pairs_main,

@@ -1,7 +1,7 @@
 """GPU checks of the precision form: the tcgen05 BF16 screening pass and the
 screened kNN against the FP64 brute-force oracle.
 
-Tolerance (spec contract): neighbour index sets equal to the FP64 answer
+Tolerance (the precision form's contract): neighbour index sets equal to the FP64 answer
 with ties broken by lower index, except swaps between candidates whose FP64
 distances differ by < 1e-6 (listed near-ties); distances within 1e-5 of FP64.
 """

@@ -772,7 +772,7 @@ __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, co
         }
     }
     // Warp reduction in double-float: a butterfly of TwoSum on the (sum, compensation)
-    // pairs, so every lane ends with the same value; one conversion to FP64 per dot.
+    // pairs, so every lane ends with the same double-float value.
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         float hi = s[c], lo = comp[c];

@@ -1,0 +1,135 @@
+"""Soundness of the certified FP32 bounds of the survivor pass (ct_screen.cu:
+warp_dots_f32 + pair_bounds_f32 and the per-query constants of two_level_topk), checked on
+the CPU.
+
+The kernel's float32 arithmetic is restated operation by operation in numpy: each of the
+32 lanes runs an FMA chain over its m/32 contiguous elements, a butterfly of additions
+joins them, and the kernel value comes from the scaled f32 coordinates.  __expf is taken
+at both ends of its documented error band (2 + floor(1.2 |x|) ulp, a little wider than
+the CUDA documentation states).  The test asserts that the FP64 value of d^2 = 1 - |rho|
+(the oracle's definition over the stored f32 inputs) lies inside [dl2, du2] for random
+pairs, pairs with tiny residual variance (inducing rows) and near-duplicate points, for
+both kernels.  A candidate is discarded on these bounds alone, so a bound that misses the
+truth would drop a true neighbour.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+F = np.float32
+
+
+def fma32(a, b, c):
+    # single rounding of a*b + c (the product of two floats is exact in double)
+    return F(np.float64(a) * np.float64(b) + np.float64(c))
+
+
+def expf_band(x):
+    e = F(np.exp(np.float64(x)))
+    u = int(2 + np.floor(1.2 * abs(float(x))))
+    lo = hi = e
+    for _ in range(u):
+        lo = np.nextafter(lo, F(-np.inf))
+        hi = np.nextafter(hi, F(np.inf))
+    return (e, lo, hi)
+
+
+def dot_f32(vq, vc, m):
+    per = m // 32
+    s = np.zeros(32, dtype=F)
+    for lane in range(32):
+        acc = F(0.0)
+        for t in range(per):
+            acc = fma32(vq[lane * per + t], vc[lane * per + t], acc)
+        s[lane] = acc
+    for off in (16, 8, 4, 2, 1):
+        s = np.array([F(s[ln] + s[ln ^ off]) for ln in range(32)], dtype=F)
+    return s[0]
+
+
+def bounds(q, c, data, exp_pick):
+    """[dl2, du2] of the pair as the kernel computes them (exp_pick: 0 nominal, 1 low, 2 high)."""
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    dot = dot_f32(Vf[q], Vf[c], m)
+    ed_q = F(F(F((m >> 5) + 7) * F(5.97e-8)) * vn[q])
+    ed = F(ed_q * vn[c])
+    dd = F(d)
+    ced2 = F(F(dd + F(2.0)) * F(5.97e-8))
+    A = F(F(2.4e-7) * F(xmax[q] + xmax_max))
+    ale = F(F(ced2 + F(F(F(0.5) * A) * dd)) * F(1.00001))
+    bee = F(F(F(0.5) * A) * F(1.00001))
+    alk = F(F(F(F(6e-8) + F(F(0.5) * ced2)) + F(F(F(0.25) * A) * dd)) * F(1.00001))
+    bek = F(F(F(1e-6) + F(F(0.25) * A)) * F(1.00001))
+    d2 = F(0.0)
+    for a in range(d):
+        t = F(xs[c, a] - xs[q, a])
+        d2 = fma32(t, t, d2)
+    if kt == 0:
+        e = expf_band(F(F(-0.5) * d2))[exp_pick]
+        kv = F(F(var) * e)
+        ek = F(kv * fma32(alk, d2, bek))
+    else:
+        ed2 = fma32(ale, d2, bee)
+        a = F(F(2.2360679775) * F(np.sqrt(d2)))
+        ea = expf_band(F(-a))[exp_pick]
+        kv = F(F(F(var) * F(F(F(1.0) + a) + F(F(a * a) * F(0.33333334)))) * ea)
+        t1 = F(kv * F(F(1e-6) + F(F(2.4e-7) * a)))
+        t2 = F(F(F(F(var) * F(F(F(0.8334) * ed2) + F(F(F(1e-7) * a) * a))) * F(F(1.0) + a)) * ea)
+        ek = F(t1 + t2)
+    R = F(abs(F(kv - dot)))
+    e = F(F(ed + ek) + fma32(R, F(1.2e-7), F(1e-30)))
+    sc = min(F(isp[q] * isp[c]), F(1e9))
+    rl = F(F(max(F(R - e), F(0.0)) * sc) * F(1.0 - 2e-6))
+    rh = F(F(F(R + e) * sc) * F(1.0 + 2e-6))
+    du2 = F(1.0) - min(rl, F(1.0))
+    dl2 = max(F(1.0) - min(rh, F(1.0)), F(0.0))
+    return float(dl2), float(du2)
+
+
+def _case(n, d, m, kt, ls, seed, dup=8):
+    r = np.random.default_rng(seed)
+    X = r.standard_normal((n, d)).astype(np.float32)
+    # near-duplicates: the last rows copy earlier ones with 1e-4 perturbations
+    X[n - dup:] = X[:dup] + F(1e-4) * r.standard_normal((dup, d)).astype(np.float32)
+    V, p, idx, _ = O.build_residual_backend_np(X, seed=seed + 1, inducing_count=m, variance=1.0, lengthscale=ls,
+                                               kernel_type=kt)
+    V = V.astype(np.float32)
+    p = p.astype(np.float32)
+    xs = (X * F(1.0 / ls)).astype(np.float32)
+    vn = np.array([np.nextafter(F(np.sqrt(np.sum(V[i].astype(np.float64) ** 2))), F(np.inf)) for i in range(n)],
+                  dtype=np.float32)
+    isp = (1.0 / np.sqrt(p.astype(np.float64))).astype(np.float32)
+    xmax = np.max(np.abs(xs), axis=1).astype(np.float32)
+    data = (V, xs, vn, isp, xmax, F(xmax.max()), 1.0, kt, m, d)
+    return X, V, p, idx, data
+
+
+@pytest.mark.parametrize("n,d,m,kt,ls", [
+    (1500, 3, 64, 1, 1.0),   # Matern 5/2, serving-like
+    (1500, 8, 64, 0, 2.0),   # RBF, precision-workload-like
+    (1200, 3, 128, 0, 0.7),  # RBF, short lengthscale, m % 128 == 0 (float4 lane shares)
+    (1200, 5, 96, 1, 2.0),   # Matern, m % 128 != 0 (scalar lane shares)
+])
+def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls):
+    X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m)
+    r = np.random.default_rng(7)
+    pairs = [tuple(r.choice(n, 2, replace=False)) for _ in range(120)]
+    pairs += [(int(idx[i]), int(j)) for i, j in zip(range(0, len(idx), max(1, len(idx) // 12)),
+                                                      r.choice(n, 12, replace=False))]  # tiny-p queries
+    pairs += [(int(j), int(idx[i])) for i, j in zip(range(0, len(idx), max(1, len(idx) // 12)),
+                                                      r.choice(n, 12, replace=False))]  # tiny-p candidates
+    pairs += [(i, n - 8 + i) for i in range(8)]                                          # near-duplicates
+    ls_vec = np.full(d, ls, np.float32)
+    widths = []
+    for i, (q, c) in enumerate(pairs):
+        if q == c:
+            continue
+        truth = float(O.residual_dist_f64(V, p, X, 1.0, ls_vec, kt, [q], [c])[0, 0]) ** 2
+        for pick in (0, 1, 2):
+            dl2, du2 = bounds(q, c, data, pick)
+            assert dl2 <= truth <= du2, (q, c, pick, dl2, truth, du2)
+        if i < 120:
+            widths.append(du2 - dl2)
+    # not vacuous: the random pairs' bounds are narrow (the filter decides them)
+    assert np.median(widths) < 1e-3, np.median(widths)

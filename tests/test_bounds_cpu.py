@@ -1,6 +1,7 @@
-"""Soundness of the certified FP32 bounds of the survivor pass (ct_screen.cu:
-warp_dots_f32 + pair_bounds_f32 and the per-query constants of two_level_topk), checked on
-the CPU.
+"""Soundness of the certified bounds of the precision form, checked on the CPU: the FP32
+filter of the survivor pass (ct_screen.cu: warp_dots_f32 + pair_bounds_f32 and the
+per-query constants of two_level_topk) and the sweep epilogue's bounds on |rho| for any
+tensor-core dot within the certified BF16 error band (screen_sweep_kernel, phase 1).
 
 The kernel's float32 arithmetic is restated operation by operation in numpy: each of the
 32 lanes runs an FMA chain over its m/32 contiguous elements, a butterfly of additions
@@ -133,3 +134,73 @@ def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls):
             widths.append(du2 - dl2)
     # not vacuous: the random pairs' bounds are narrow (the filter decides them)
     assert np.median(widths) < 1e-3, np.median(widths)
+
+
+def epilogue_rho_bounds(q, c, data, v_mma, exp_pick):
+    """Lower / upper bounds of |rho| the sweep epilogue derives for one pair from a tensor-core
+    dot v_mma: the heap uses max(blo, 0) isq (1 - 1e-6), the survivor test bhi isq / (1 - 2e-6)."""
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    u2 = 1.0 / 65536.0
+    err_coef = F(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22)
+    err_c = F(err_coef * vn[c])
+    vnq, isq, isc = vn[q], isp[q], isp[c]
+    dd = F(d)
+    ced2 = F(F(dd + F(2.0)) * F(5.97e-8))
+    A = F(F(2.4e-7) * F(xmax[q] + xmax_max))
+    ale = F(F(ced2 + F(F(F(0.5) * A) * dd)) * F(1.00001))
+    bee = F(F(F(0.5) * A) * F(1.00001))
+    alk = F(F(F(F(6e-8) + F(F(0.5) * ced2)) + F(F(F(0.25) * A) * dd)) * F(1.00001))
+    bek = F(F(F(1e-6) + F(F(0.25) * A)) * F(1.00001))
+    d2 = F(0.0)
+    for a in range(d):
+        t = F(xs[c, a] + F(-xs[q, a]))
+        d2 = fma32(t, t, d2)
+    if kt == 0:
+        e = expf_band(F(F(-0.5) * d2))[exp_pick]
+        kv = F(F(var) * e)
+        ek = F(kv * fma32(alk, d2, bek))
+    else:
+        ed2 = fma32(ale, d2, bee)
+        a = F(F(2.2360679775) * F(np.sqrt(d2)))
+        ea = expf_band(F(-a))[exp_pick]
+        kv = F(F(F(var) * F(F(F(1.0) + a) + F(F(a * a) * F(0.33333334)))) * ea)
+        t1 = F(kv * F(F(1e-6) + F(F(2.4e-7) * a)))
+        t2 = F(F(F(F(var) * F(F(F(0.8334) * ed2) + F(F(F(1e-7) * a) * a))) * F(F(1.0) + a)) * ea)
+        ek = F(t1 + t2)
+    R = F(abs(F(kv + F(-v_mma))))
+    e = F(fma32(vnq, err_c, ek) + fma32(R, F(1.2e-7), F(1e-30)))
+    blo = F(F(R + F(-e)) * isc)
+    bhi = F(F(R + e) * isc)
+    rho_lo = float(F(F(max(blo, F(0.0)) * isq) * F(1.0 - 1e-6)))
+    rho_hi = float(bhi) * float(isq) / (1.0 - 2e-6)
+    return rho_lo, rho_hi
+
+
+@pytest.mark.parametrize("n,d,m,kt,ls", [
+    (1500, 3, 64, 1, 1.0),
+    (1500, 8, 64, 0, 2.0),
+    (1200, 3, 128, 0, 0.7),
+])
+def test_epilogue_bounds_contain_fp64(n, d, m, kt, ls):
+    """The sweep's bounds on |rho| for a tensor-core dot anywhere in its certified BF16 error
+    band (c_split |v_q| |v_c| around the exact dot) contain the FP64 |rho|."""
+    X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m + 1)
+    vn = data[2]
+    u2 = 1.0 / 65536.0
+    c_split = 3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22
+    r = np.random.default_rng(11)
+    pairs = [tuple(r.choice(n, 2, replace=False)) for _ in range(100)]
+    pairs += [(int(idx[i]), int(j)) for i, j in zip(range(0, len(idx), max(1, len(idx) // 10)),
+                                                      r.choice(n, 10, replace=False))]
+    pairs += [(i, n - 8 + i) for i in range(8)]
+    ls_vec = np.full(d, ls, np.float32)
+    for q, c in pairs:
+        if q == c:
+            continue
+        rho_true = 1.0 - float(O.residual_dist_f64(V, p, X, 1.0, ls_vec, kt, [q], [c])[0, 0]) ** 2
+        exact = float(np.dot(V[q].astype(np.float64), V[c].astype(np.float64)))
+        band = c_split * float(vn[q]) * float(vn[c])
+        for v_mma in (F(exact), F(exact - band), F(exact + band)):
+            for pick in (0, 1, 2):
+                lo, hi = epilogue_rho_bounds(q, c, data, v_mma, pick)
+                assert lo <= rho_true <= hi, (q, c, float(v_mma), pick, lo, rho_true, hi)

@@ -191,6 +191,81 @@ def run_reference(args, wl):
     print(json.dumps(line))
 
 
+# ------------------------------------------------------------------ FP64 check of the timed output
+def fp64_check(wl, dev, rows, got_idx, got_dist, near_tie=1e-6, block=256):
+    """Check the neighbour rows of query ids `rows` (int64 numpy) produced by the timed
+    run against an FP64 brute force evaluated here with torch on the GPU (independent
+    of the engine's kernels): x/l, the RBF or Matern 5/2 kernel, rho = (K - v_q.v_c) /
+    sqrt(max(p_q p_c, 1e-18)) clamped to [-1, 1], d = sqrt(1 - |rho|), d(q, q) = 0;
+    order (d, idx).  A row whose set differs is a near-tie row when every swapped pair
+    of candidates is closer than `near_tie` in FP64 distance, else a mismatch."""
+    import torch
+
+    f64 = torch.float64
+    inv_ls = 1.0 / torch.tensor([wl.lengthscale] * wl.d, dtype=f64, device=dev)
+    X = torch.as_tensor(wl.coords, device=dev).to(f64) * inv_ls
+    V = torch.as_tensor(wl.v, device=dev).to(f64)
+    P = torch.as_tensor(wl.p, device=dev).to(f64)
+    k = wl.k
+    rows = np.asarray(rows, dtype=np.int64)
+    order = np.argsort(rows, kind="stable")
+    stats = {"queries": int(rows.size), "rows_identical": 0, "near_tie_rows": 0, "mismatches_beyond_near_tie": 0,
+             "count_mismatches": 0, "max_abs_err": 0.0, "predecessor_violations": 0, "near_tie": near_tie,
+             "oracle": "FP64 brute force (torch, GPU) over the stored f32 V, p and coordinates"}
+    for s in range(0, rows.size, block):
+        sel = order[s:s + block]
+        q = torch.as_tensor(rows[sel], device=dev)
+        hi = int(rows[sel].max()) if wl.predecessor else wl.n
+        if hi <= 0:
+            continue
+        xc = X[:hi]
+        d2 = torch.zeros((q.numel(), hi), dtype=f64, device=dev)
+        for a in range(wl.d):
+            d2 += (X[q, a][:, None] - xc[:, a][None, :]) ** 2
+        if wl.kernel_type == 1:
+            t = np.sqrt(5.0) * torch.sqrt(d2)
+            K = wl.variance * (1.0 + t + t * t / 3.0) * torch.exp(-t)
+        else:
+            K = wl.variance * torch.exp(-0.5 * d2)
+        K -= V[q] @ V[:hi].T
+        K /= torch.sqrt(torch.clamp(P[q][:, None] * P[:hi][None, :], min=1e-18))
+        D = torch.sqrt(torch.clamp(1.0 - torch.abs(torch.clamp(K, -1.0, 1.0)), min=0.0))
+        cols = torch.arange(hi, device=dev)
+        D[q[:, None] == cols[None, :]] = 0.0
+        if wl.predecessor:
+            D[cols[None, :] >= q[:, None]] = float("inf")
+        dv, di = torch.sort(D, dim=1, stable=True)
+        dv, di = dv[:, :k].cpu().numpy(), di[:, :k].cpu().numpy()
+        Dh = None
+        for r_local, r in enumerate(sel):
+            fin = np.isfinite(dv[r_local])
+            ref = set(int(x) for x in di[r_local][fin])
+            gi = got_idx[r]
+            got = set(int(x) for x in gi if x >= 0)
+            if (gi >= 0).sum() != fin.sum():
+                stats["count_mismatches"] += 1
+            if wl.predecessor and np.any(gi[gi >= 0] >= rows[r]):
+                stats["predecessor_violations"] += 1
+            nv = int(min((gi >= 0).sum(), fin.sum()))
+            if nv:
+                err = float(np.abs(got_dist[r][:nv].astype(np.float64) - dv[r_local][:nv]).max())
+                stats["max_abs_err"] = max(stats["max_abs_err"], err)
+            if got == ref:
+                stats["rows_identical"] += 1
+                continue
+            if Dh is None:
+                Dh = D.cpu().numpy()
+            eg, ef = sorted(got - ref), sorted(ref - got)
+            gap = np.inf if len(eg) != len(ef) or max(eg + ef) >= hi else float(
+                np.max(np.abs(np.sort(Dh[r_local, eg]) - np.sort(Dh[r_local, ef]))))
+            if gap < near_tie:
+                stats["near_tie_rows"] += 1
+            else:
+                stats["mismatches_beyond_near_tie"] += 1
+        del d2, K, D
+    return stats
+
+
 # ------------------------------------------------------------------ batching form
 def fp32_core_peak(sm_mhz):
     """Separately rounded FP32 multiply + add throughput of the CUDA cores (the plain
@@ -418,6 +493,13 @@ def main():
     value = q_total / (ms_per_step / 1e3)
     screened_idx = idx_out.clone()
     screened_dist = dist_out.clone()
+    # FP64 check of the last timed step's output on 4096 sampled queries
+    fp64 = None
+    if world == 1:
+        sample = np.random.default_rng(4).choice(wl.n, min(4096, wl.n), replace=False)
+        fp64 = fp64_check(wl, dev, sample, screened_idx[sample].cpu().numpy(), screened_dist[sample].cpu().numpy())
+        fp64["sample"] = "default_rng(4).choice(N, 4096, replace=False) rows of the last timed step"
+        torch.cuda.empty_cache()
 
     # ---- e2e through the host-facing call (pinned host buffers, copies timed)
     q_pin = torch.as_tensor(q_host).pin_memory()
@@ -470,8 +552,8 @@ def main():
     alg_flops = 2.0 * wl.m * pairs_main             # per-unit figure 2m flops per screened pair
     issued_flops = 3.0 * alg_flops                  # hi.hi + hi.lo + lo.hi
     achieved = alg_flops / (screen_ms / 1e3) / 1e12
-    # DRAM bytes per screened pair of the sweep, from the ncu capture at N=65536 of the
-    # same workload (profiles/screen_sweep_precision_workload.md), scaled to this launch
+    # DRAM bytes per screened pair of the sweep, from an ncu capture of the same kernel on
+    # the N=65536 case of this workload, scaled to this launch
     sweep_dram_bytes_per_pair = 7.19
     roofline = {
         "bound": "tensor", "kernel": "screen_sweep_kernel (main sweep)", "achieved": achieved,
@@ -542,6 +624,7 @@ def main():
             "plain_fp32": plain,
             "speedup_vs_plain_fp32": (value / plain["value"]) if plain else None,
             "neighbour_agreement_vs_plain": agree,
+            "fp64_check": fp64,
             "wall_s_timed": t_wall,
             "batching": batching,
             "serving": serving,

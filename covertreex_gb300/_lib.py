@@ -24,6 +24,7 @@ CT_KERNEL_RBF = 0
 CT_KERNEL_MATERN52 = 1
 CT_ORDER_NATURAL = 0
 CT_ORDER_HILBERT = 1
+CT_ORDER_MORTON = 2
 CT_FORM_DENSE = 0
 CT_FORM_TREE = 1
 CT_FORM_SCREENED = 2
@@ -64,6 +65,8 @@ EXPORTED_SYMBOLS = (
     "ct_batch_get_shape",
     "ct_batch_reserve",
     "ct_batch_free",
+    "ct_batch_order",
+    "ct_luby_mis",
 )
 
 
@@ -176,6 +179,10 @@ def load(build_if_missing: bool = True):
         L.ct_batch_reserve.argtypes = [vp, i32, i32, i32]
         L.ct_batch_free.restype = ctypes.c_int
         L.ct_batch_free.argtypes = [vp]
+        L.ct_batch_order.restype = ctypes.c_int
+        L.ct_batch_order.argtypes = [vp, i64, i32, i32, vp, vp]
+        L.ct_luby_mis.restype = ctypes.c_int
+        L.ct_luby_mis.argtypes = [vp, vp, i64, u64, vp, ip32, vp]
         _handle = L
         return L
 

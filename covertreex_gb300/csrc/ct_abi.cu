@@ -230,6 +230,63 @@ int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* c
     return rc == CT_OK ? CT_OK : fail(rc, "ct_knn_residual_dense_noalloc: %s", msg);
 }
 
+namespace {
+__global__ void widen_order_kernel(const int* __restrict__ in, long long n, long long* __restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+__global__ void iota_kernel(long long n, long long* __restrict__ out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = i;
+}
+}  // namespace
+
+int ct_batch_order(const float* coords, int64_t n, int32_t d, int32_t mode, int64_t* out_perm, void* stream) {
+    if (n < 0 || n >= (1LL << 31)) return fail(CT_ERR_ARG, "ct_batch_order: n=%lld outside [0, 2^31)", (long long)n);
+    if (d <= 0 || d > 64) return fail(CT_ERR_ARG, "ct_batch_order: d=%d outside [1, 64]", d);
+    if (mode != CT_ORDER_NATURAL && mode != CT_ORDER_HILBERT && mode != CT_ORDER_MORTON)
+        return fail(CT_ERR_ARG, "ct_batch_order: unknown mode %d", mode);
+    if (n == 0) return CT_OK;
+    if (!coords || !out_perm) return fail(CT_ERR_ARG, "ct_batch_order: NULL pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    // the reference's Morton order is defined for D = 3 only and is the identity otherwise
+    if (mode == CT_ORDER_NATURAL || (mode == CT_ORDER_MORTON && d != 3)) {
+        iota_kernel<<<grid, 256, 0, st>>>(n, (long long*)out_perm);
+        CT_CUDA(cudaGetLastError(), "ct_batch_order");
+        return CT_OK;
+    }
+    int* order32 = nullptr;
+    CT_CUDA(cudaMallocAsync((void**)&order32, sizeof(int) * (size_t)n, st), "ct_batch_order allocation");
+    cudaError_t e = ct::compute_order(coords, n, d, mode == CT_ORDER_MORTON ? 2 : 1, order32, st);
+    if (e == cudaSuccess) {
+        widen_order_kernel<<<grid, 256, 0, st>>>(order32, n, (long long*)out_perm);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(order32, st);
+    if (e != cudaSuccess) return cuda_fail(e, "ct_batch_order");
+    return CT_OK;
+}
+
+int ct_luby_mis(const int64_t* indptr, const int64_t* indices, int64_t n, uint64_t seed, int8_t* out_sel,
+                int32_t* iterations, void* stream) {
+    if (iterations) *iterations = 0;
+    if (n < 0) return fail(CT_ERR_ARG, "ct_luby_mis: n < 0");
+    if (n == 0) return CT_OK;
+    if (!indptr || !out_sel) return fail(CT_ERR_ARG, "ct_luby_mis: NULL pointer");
+    cudaStream_t st = (cudaStream_t)stream;
+    bool valid = false;
+    CT_CUDA(ct::csr_graph_valid((const long long*)indptr, (const long long*)indices, n, &valid, st), "ct_luby_mis");
+    if (!valid)
+        return fail(CT_ERR_ARG, "ct_luby_mis: indptr must start at 0 and not decrease, indices must lie in [0, n)");
+    int it = 0;
+    CT_CUDA(ct::luby_mis_csr((const long long*)indptr, (const long long*)indices, n, seed, (signed char*)out_sel, &it,
+                             st),
+            "ct_luby_mis");
+    if (iterations) *iterations = it;
+    return CT_OK;
+}
+
 int ct_tree_inputs(const ct_tree* T, float* v, float* p, float* coords, void* stream) {
     if (!T) return fail(CT_ERR_ARG, "ct_tree_inputs: tree is NULL");
     cudaStream_t st = (cudaStream_t)stream;

@@ -41,6 +41,12 @@ cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long 
                              bool* result_in_tmp);
 int radix_num_blocks(long long n);
 
+// ct_mis.cu
+cudaError_t csr_graph_valid(const long long* indptr, const long long* indices, long long n, bool* valid,
+                            cudaStream_t st);
+cudaError_t luby_mis_csr(const long long* indptr, const long long* indices, long long n, unsigned long long seed,
+                         signed char* sel, int* iterations, cudaStream_t st);
+
 // ct_euclid.cu
 cudaError_t launch_euclid_knn(const float* pts, long long n, int d, const float* qry, long long nq, int k,
                               int predecessor, long long* out_idx, float* out_dist, cudaStream_t st);

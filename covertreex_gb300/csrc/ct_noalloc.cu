@@ -10,6 +10,7 @@
 // p copy, 1/lengthscale) lives in one file-scope __device__ array of fixed size,
 // reserved when the library is loaded and held by every GPU that loads it until
 // the process exits.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -25,9 +26,15 @@ namespace {
 constexpr size_t kScratchBytes = (size_t)CT_NOALLOC_SCRATCH_BYTES;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device addresses of g_noalloc_scratch, looked up once per device.
+// Device addresses of g_noalloc_scratch, looked up once per CUDA context and kept
+// under the context's unique id (cuCtxGetId ids are never reused), so that a context
+// destroyed by cudaDeviceReset, or a caller's own non-primary context on the same
+// device, gets its own lookup instead of a stale address.
 std::mutex g_mu;
-void* g_scratch_addr[128] = {nullptr};
+constexpr int kCacheSlots = 64;
+unsigned long long g_ctx_id[kCacheSlots] = {0};
+void* g_scratch_addr[kCacheSlots] = {nullptr};
+int g_next_slot = 0;
 
 struct InvLs {
     float v[64];
@@ -42,29 +49,67 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
+// Scratch bytes a call needs: five pieces, each rounded up to a multiple of 256
+// bytes — V in residue-major order (4 n m), scaled coordinates (4 n d), squared norms
+// (4 n), p (4 n) and the inverse lengthscales (256).
 size_t ct_noalloc_bytes_needed(long long n, int m, int d) {
     return align256((size_t)n * m * 4) + align256((size_t)n * d * 4) + align256((size_t)n * 4) +
            align256((size_t)n * 4) + align256(64 * 4);
 }
 
-// Scratch address for the current device: cudaGetSymbolAddress on first use
-// (with that device current), cached afterwards.
-static int noalloc_scratch(void** out, char* err, size_t errlen) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) { snprintf(err, errlen, "cudaGetDevice: %s", cudaGetErrorString(e)); return CT_ERR_CUDA; }
-    if (dev < 0 || dev >= 128) { snprintf(err, errlen, "device ordinal %d out of range", dev); return CT_ERR_ARG; }
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) {
-            snprintf(err, errlen, "cudaGetSymbolAddress(no-allocation scratch): %s", cudaGetErrorString(e));
-            return CT_ERR_CUDA;
+// Unique id of the calling thread's current CUDA context (0 if none or unknown).  The
+// two driver functions are fetched through the runtime, so the library does not link
+// the driver library itself (it still loads on machines without a GPU driver).
+static unsigned long long current_context_id() {
+    typedef CUresult (*get_current_fn)(CUcontext*);
+    typedef CUresult (*get_id_fn)(CUcontext, unsigned long long*);
+    static get_current_fn get_current = nullptr;
+    static get_id_fn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess) {
+            get_current = (get_current_fn)a;
+            get_id = (get_id_fn)b;
         }
-        g_scratch_addr[dev] = ptr;
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+        return id;
+    return 0;
+}
+
+// Scratch address in the calling thread's current context: cudaGetSymbolAddress on
+// the first call in a context (which also creates the device's primary context when
+// none is current), cached by context id afterwards.
+static int noalloc_scratch(void** out, char* err, size_t errlen) {
+    unsigned long long id = current_context_id();
+    if (id) {
+        std::lock_guard<std::mutex> lock(g_mu);
+        for (int i = 0; i < kCacheSlots; ++i)
+            if (g_ctx_id[i] == id) { *out = g_scratch_addr[i]; return CT_OK; }
     }
-    *out = g_scratch_addr[dev];
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+        snprintf(err, errlen, "cudaGetSymbolAddress(no-allocation scratch): %s", cudaGetErrorString(e));
+        return CT_ERR_CUDA;
+    }
+    // the lookup made the runtime's context current if none was: key the cache by it
+    id = current_context_id();
+    if (id) {
+        std::lock_guard<std::mutex> lock(g_mu);
+        g_ctx_id[g_next_slot] = id;
+        g_scratch_addr[g_next_slot] = ptr;
+        g_next_slot = (g_next_slot + 1) % kCacheSlots;
+    }
+    *out = ptr;
     return CT_OK;
 }
 

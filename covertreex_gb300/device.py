@@ -398,3 +398,44 @@ def build_vmatrix_cuda(points: np.ndarray, inducing_idx: np.ndarray, *, kernel_t
     finally:
         f.free()
     return V, p, L
+
+
+_ORDER_MODES = {"natural": _lib.CT_ORDER_NATURAL, "hilbert": _lib.CT_ORDER_HILBERT, "morton": _lib.CT_ORDER_MORTON}
+
+
+def batch_order(coords, mode: str = "hilbert", device=None) -> np.ndarray:
+    """Stable batch order of points on the GPU (``ct_batch_order``).
+
+    ``mode="hilbert"``: the Python PCCT path's Hilbert permutation
+    (covertreex/algo/order/strategy.py:38-100); ``mode="morton"``: the Rust crate's
+    ``hilbert_order`` (src/lib.rs:954-962, src/pcct.rs:27-67; identity unless D = 3)."""
+    torch = _torch()
+    if mode not in _ORDER_MODES:
+        raise ValueError(f"unknown order mode {mode!r}")
+    dev = torch.device(device if device is not None else "cuda")
+    c = _as_device(coords, torch.float32, dev)
+    if c.dim() == 1:
+        c = c.reshape(-1, 1)
+    n, d = int(c.shape[0]), int(c.shape[1])
+    out = torch.empty(n, dtype=torch.int64, device=dev)
+    _lib.check(_lib.load().ct_batch_order(c.data_ptr(), n, d, _ORDER_MODES[mode], out.data_ptr(), _stream_ptr(None)))
+    return out.cpu().numpy()
+
+
+def luby_mis(indptr, indices, seed: int, device=None):
+    """Maximal independent set of a CSR conflict graph on the GPU (``ct_luby_mis``), with
+    run_mis_numba's semantics (covertreex/algo/_mis_numba.py:64-140).  Returns
+    (int8 indicator, iterations)."""
+    torch = _torch()
+    dev = torch.device(device if device is not None else "cuda")
+    ip = _as_device(np.asarray(indptr, dtype=np.int64), torch.int64, dev)
+    ix = _as_device(np.asarray(indices, dtype=np.int64).reshape(-1), torch.int64, dev)
+    n = int(ip.numel()) - 1
+    if n < 0:
+        raise ValueError("indptr must hold n + 1 entries")
+    sel = torch.zeros(max(n, 1), dtype=torch.int8, device=dev)
+    it = ctypes.c_int32(0)
+    _lib.check(_lib.load().ct_luby_mis(ip.data_ptr(), ix.data_ptr() if ix.numel() else None, n,
+                                       int(seed) & 0xFFFFFFFFFFFFFFFF, sel.data_ptr(), ctypes.byref(it),
+                                       _stream_ptr(None)))
+    return sel[:n].cpu().numpy(), int(it.value)

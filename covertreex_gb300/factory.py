@@ -43,6 +43,11 @@ class BuiltCoverTree:
 
     @property
     def build_time(self) -> Optional[float]:
+        """Seconds spent building the device index.  The default search forms (screened,
+        dense) need no cover tree, so by default no tree is built and this is the time of
+        the device-resident metric setup (V relayout, scaled coordinates, norms, copies);
+        the reference's ``build_time`` counts its Rust tree build instead.  The cover tree
+        itself is built only for the tree form."""
         return self._tree.build_seconds
 
     def __repr__(self) -> str:

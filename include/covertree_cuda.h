@@ -53,9 +53,13 @@ extern "C" {
 #define CT_KERNEL_RBF 0
 #define CT_KERNEL_MATERN52 1
 
-/* order: batch order of the build (src/lib.rs:1398-1405 batch_order). */
+/* order: batch order of the build (src/lib.rs:1398-1405 batch_order).
+ *   CT_ORDER_HILBERT: the Python PCCT path's Hilbert curve (covertreex/algo/order/strategy.py:38-100)
+ *   CT_ORDER_MORTON:  the Rust crate's `hilbert_like_order` (src/pcct.rs:27-67), a 3-D Morton code,
+ *                     the identity for D != 3 */
 #define CT_ORDER_NATURAL 0
 #define CT_ORDER_HILBERT 1
+#define CT_ORDER_MORTON 2
 
 /* form: which search ct_knn_residual runs; all return the same neighbour contract. */
 #define CT_FORM_DENSE 0     /* plain FP32, dense sweep, bit-exact reference f32 distances */
@@ -135,18 +139,45 @@ CT_API int ct_knn_euclidean(const float* points, int64_t n, int32_t d, const flo
  * into the caller's outputs (out_idx [nq x k] int64, out_dist [nq x k] f32; device).
  * lengthscale is a HOST pointer, as in ct_build_residual.
  * Scratch: one fixed __device__ array of CT_NOALLOC_SCRATCH_BYTES (64 MiB) inside the
- * library, held by every GPU that loads it until the process exits; a call needs
- * 4 n (m + d + 2) bytes (256-byte aligned pieces) and is rejected with CT_ERR_UNSUPPORTED
- * beyond that.  The first call on a device looks up the array's device address.  All
- * calls share the array: calls whose GPU work overlaps (different streams, threads or
- * processes' contexts on the same device) race and must be serialised by the caller.
- * m must be a multiple of 16; k <= 128.  Allocates nothing.
+ * library, held by every GPU (every CUDA context) that loads it until the process
+ * exits.  A call needs the sum of five pieces, each rounded up to a multiple of 256
+ * bytes: 4 n m + 4 n d + 4 n + 4 n + 256 (V, scaled coordinates, norms, p, inverse
+ * lengthscales); beyond CT_NOALLOC_SCRATCH_BYTES it is rejected with CT_ERR_UNSUPPORTED
+ * before any device work.  The first call in a CUDA context looks up the array's device
+ * address (cudaGetSymbolAddress, kept for that context).  All calls in one context share
+ * the array and it keeps the last call's contents (each call writes every byte it reads):
+ * calls whose GPU work overlaps (different streams or threads) race and must be
+ * serialised by the caller.  m must be a multiple of 16; k <= 128.  Allocates nothing.
  */
 #define CT_NOALLOC_SCRATCH_BYTES (64ull << 20)
 CT_API int ct_knn_residual_dense_noalloc(const float* v, const float* p, const float* coords, int64_t n, int32_t m,
                                          int32_t d, float variance, const float* lengthscale, int32_t n_lengthscale,
                                          int32_t kernel_type, const int64_t* q_ids, int64_t nq, int32_t k,
                                          int32_t predecessor, int64_t* out_idx, float* out_dist, void* stream);
+
+/*
+ * Batch order of points: out_perm[i] = row of `coords` [n x d] (device f32) at sorted
+ * position i, stable (ties keep the lower row).  Replaces the PyO3 function
+ * hilbert_order(coords) (src/lib.rs:954-962 -> src/pcct.rs:27-67, mode CT_ORDER_MORTON)
+ * and the Python path's _hilbert_permutation (covertreex/algo/order/strategy.py:38-100,
+ * mode CT_ORDER_HILBERT; keys quantised in FP64 from the f32 coordinates).
+ * out_perm: device int64 [n].  Asynchronous except for the sort's small host copies.
+ */
+CT_API int ct_batch_order(const float* coords, int64_t n, int32_t d, int32_t mode, int64_t* out_perm, void* stream);
+
+/*
+ * Maximal independent set of a conflict graph in CSR form (indptr [n+1], indices
+ * [nnz]; device int64; symmetric adjacency expected, as the reference builds it) into
+ * out_sel (device int8 [n], 1 = selected).  Replaces run_mis_numba(indptr, indices,
+ * seed) (covertreex/algo/_mis_numba.py:134-140): the greedy in index order when the
+ * maximum degree is <= 8, else seeded Luby rounds with the reference's hash
+ * priorities; *iterations (host, may be NULL) receives the reference's iteration count.
+ * A malformed graph (indptr not starting at 0 or decreasing, an index outside [0, n))
+ * is rejected with CT_ERR_ARG before any kernel reads it.  Synchronises `stream` once
+ * per round.
+ */
+CT_API int ct_luby_mis(const int64_t* indptr, const int64_t* indices, int64_t n, uint64_t seed, int8_t* out_sel,
+                       int32_t* iterations, void* stream);
 
 /* Copy tree arrays to device buffers of n entries each (any may be NULL):
  * parents (node numbering), levels, si (cover radii), node_to_dataset, subtree_min. */

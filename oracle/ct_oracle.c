@@ -1269,3 +1269,167 @@ CT_EXPORT void ct_hilbert_codes(const double* pts, int64_t n, int d, uint64_t* c
         codes[i] = idx;
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* FP64 brute force (ground truth for the precision form at full size).       */
+/* Same formula as oracle.py's residual_dist_f64 over the stored f32 inputs:  */
+/* x/l in FP64, K = var exp(-d2/2) (RBF) or var (1+a+a^2/3) e^-a, a = sqrt(5  */
+/* d2) (Matern 5/2), rho = clamp((K - v_q.v_c) / sqrt(max(p_q p_c, 1e-18)),   */
+/* +-1), d = sqrt(1-|rho|), d(q,q) = 0 (src/metric.rs:376-487 in FP64).       */
+/* Queries are processed in blocks of BQ that share each candidate row, the   */
+/* dot products of f32 inputs are exact products summed in FP64.  Results are */
+/* ascending by (d, idx); rows with fewer than k candidates pad -1 / +inf.    */
+/* cand_limit: candidates are rows [0, cand_limit) (rows beyond it are new    */
+/* query points stored after the dataset).                                    */
+/* ------------------------------------------------------------------------- */
+#define BQ64 16
+typedef struct { double d; int64_t i; } nb64;
+static inline int nb64_less(nb64 a, nb64 b) { return a.d < b.d || (a.d == b.d && a.i < b.i); }
+
+CT_EXPORT void ct_oracle_brute_f64(const float* v, const float* p, const float* coords, int64_t n, int m, int d,
+                                   double var, const float* ls, int n_ls, int kernel_type,
+                                   const int64_t* queries, int64_t nq, int k, int predecessor, int64_t cand_limit,
+                                   int64_t* out_idx, double* out_dist, int n_threads) {
+    const int64_t nc = cand_limit > 0 && cand_limit < n ? cand_limit : n;
+    double inv_ls[64];
+    for (int c = 0; c < d; ++c) {
+        float raw = (ls && n_ls > 0) ? ls[c < n_ls ? c : 0] : 1.0f;
+        inv_ls[c] = 1.0 / (double)raw;
+    }
+    /* query blocks in ascending id order (predecessor mode scores [0, max id) only) */
+    int64_t* ord = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nq > 0 ? nq : 1));
+    for (int64_t i = 0; i < nq; ++i) ord[i] = i;
+    {
+        /* bottom-up merge sort of the rows by query id (stable) */
+        int64_t* tmp = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nq > 0 ? nq : 1));
+        for (int64_t w = 1; w < nq; w *= 2) {
+            for (int64_t lo = 0; lo < nq; lo += 2 * w) {
+                int64_t mid = lo + w < nq ? lo + w : nq, hi = lo + 2 * w < nq ? lo + 2 * w : nq;
+                int64_t a = lo, b = mid, o = lo;
+                while (a < mid && b < hi) tmp[o++] = queries[ord[b]] < queries[ord[a]] ? ord[b++] : ord[a++];
+                while (a < mid) tmp[o++] = ord[a++];
+                while (b < hi) tmp[o++] = ord[b++];
+            }
+            memcpy(ord, tmp, sizeof(int64_t) * (size_t)nq);
+        }
+        free(tmp);
+    }
+    const int64_t nblk = (nq + BQ64 - 1) / BQ64;
+#ifdef _OPENMP
+    if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+    (void)n_threads;
+#endif
+    #pragma omp parallel
+    {
+        double* vqt = (double*)malloc(sizeof(double) * (size_t)m * BQ64);   /* [m][BQ64] */
+        nb64* heap = (nb64*)malloc(sizeof(nb64) * (size_t)BQ64 * (size_t)(k + 1));
+        int hn[BQ64];
+        #pragma omp for schedule(dynamic, 1)
+        for (int64_t blk = 0; blk < nblk; ++blk) {
+            const int64_t b0 = blk * BQ64;
+            const int nb = (int)(nq - b0 < BQ64 ? nq - b0 : BQ64);
+            int64_t qid[BQ64];
+            double xq[BQ64][64], pq[BQ64];
+            int64_t hi = 0;
+            for (int t = 0; t < BQ64; ++t) {
+                const int64_t q = t < nb ? queries[ord[b0 + t]] : -1;
+                qid[t] = q;
+                hn[t] = 0;
+                const int ok = q >= 0 && q < n;
+                for (int j = 0; j < m; ++j) vqt[(size_t)j * BQ64 + t] = ok ? (double)v[(size_t)q * m + j] : 0.0;
+                for (int c = 0; c < d; ++c) xq[t][c] = ok ? (double)coords[(size_t)q * d + c] * inv_ls[c] : 0.0;
+                pq[t] = ok ? (double)p[q] : 1.0;
+                const int64_t lim = !ok ? 0 : (predecessor ? (q < nc ? q : nc) : nc);
+                if (lim > hi) hi = lim;
+            }
+            for (int64_t c = 0; c < hi; ++c) {
+                double acc[BQ64];
+                for (int t = 0; t < BQ64; ++t) acc[t] = 0.0;
+                const float* vc = v + (size_t)c * m;
+                for (int j = 0; j < m; ++j) {
+                    const double x = (double)vc[j];
+                    const double* row = vqt + (size_t)j * BQ64;
+                    for (int t = 0; t < BQ64; ++t) acc[t] += row[t] * x;
+                }
+                double xc[64];
+                for (int a = 0; a < d; ++a) xc[a] = (double)coords[(size_t)c * d + a] * inv_ls[a];
+                const double pc = (double)p[c];
+                for (int t = 0; t < nb; ++t) {
+                    const int64_t q = qid[t];
+                    if (q < 0 || q >= n) continue;
+                    if (predecessor ? c >= q : 0) continue;
+                    double dd;
+                    if (c == q) {
+                        dd = 0.0;
+                    } else {
+                        double d2 = 0.0;
+                        for (int a = 0; a < d; ++a) { const double df = xq[t][a] - xc[a]; d2 += df * df; }
+                        double K;
+                        if (kernel_type == 1) {
+                            const double aa = sqrt(5.0) * sqrt(d2);
+                            K = var * (1.0 + aa + aa * aa / 3.0) * exp(-aa);
+                        } else {
+                            K = var * exp(-0.5 * d2);
+                        }
+                        double pp = pq[t] * pc;
+                        if (pp < 1e-18) pp = 1e-18;
+                        double rho = (K - acc[t]) / sqrt(pp);
+                        if (rho > 1.0) rho = 1.0;
+                        if (rho < -1.0) rho = -1.0;
+                        const double om = 1.0 - fabs(rho);
+                        dd = sqrt(om > 0.0 ? om : 0.0);
+                    }
+                    /* bounded max-heap of the k best (d, idx) */
+                    nb64* h = heap + (size_t)t * (k + 1);
+                    const nb64 x = {dd, c};
+                    if (hn[t] < k) {
+                        int i = hn[t]++;
+                        while (i > 0) { int pa = (i - 1) / 2; if (!nb64_less(h[pa], x)) break; h[i] = h[pa]; i = pa; }
+                        h[i] = x;
+                    } else if (nb64_less(x, h[0])) {
+                        int i = 0;
+                        for (;;) {
+                            int l = 2 * i + 1, r = l + 1, g = i;
+                            nb64 hg = x;
+                            if (l < k && nb64_less(hg, h[l])) { g = l; hg = h[l]; }
+                            if (r < k && nb64_less(hg, h[r])) { g = r; }
+                            if (g == i) break;
+                            h[i] = h[g];
+                            i = g;
+                        }
+                        h[i] = x;
+                    }
+                }
+            }
+            for (int t = 0; t < nb; ++t) {
+                nb64* h = heap + (size_t)t * (k + 1);
+                /* heap sort ascending */
+                for (int e = hn[t] - 1; e > 0; --e) {
+                    nb64 top = h[0];
+                    nb64 x = h[e];
+                    int i = 0;
+                    for (;;) {
+                        int l = 2 * i + 1, r = l + 1, g = i;
+                        nb64 hg = x;
+                        if (l < e && nb64_less(hg, h[l])) { g = l; hg = h[l]; }
+                        if (r < e && nb64_less(hg, h[r])) { g = r; }
+                        if (g == i) break;
+                        h[i] = h[g];
+                        i = g;
+                    }
+                    h[i] = x;
+                    h[e] = top;
+                }
+                const int64_t row = ord[b0 + t];
+                for (int j = 0; j < k; ++j) {
+                    out_idx[row * k + j] = j < hn[t] ? h[j].i : -1;
+                    out_dist[row * k + j] = j < hn[t] ? h[j].d : INFINITY;
+                }
+            }
+        }
+        free(vqt);
+        free(heap);
+    }
+    free(ord);
+}

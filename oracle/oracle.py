@@ -99,6 +99,10 @@ def lib():
     L.ct_oracle_luby_mis.argtypes = [_i64p, _i64p, ctypes.c_int64, ctypes.c_int64, _i8p]
     L.ct_hilbert_codes.restype = None
     L.ct_hilbert_codes.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int, _u64p]
+    L.ct_oracle_brute_f64.restype = None
+    L.ct_oracle_brute_f64.argtypes = [_f32p, _f32p, _f32p, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, _f32p, ctypes.c_int, ctypes.c_int, _i64p, ctypes.c_int64,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int64, _i64p, _f64p, ctypes.c_int]
     _lib = L
     return L
 
@@ -152,23 +156,32 @@ def build_residual_backend_np(points, *, seed: int, inducing_count: int, varianc
 # --------------------------------------------------------------------------
 def residual_dist_f64(V, p, coords, var, ls, kernel_type, qi, cj):
     """FP64 residual distance sqrt(1-|rho|) over the stored f32 inputs, for rows qi x cols cj."""
-    V = np.asarray(V, dtype=np.float64)
-    X = np.asarray(coords, dtype=np.float64) / np.asarray(ls, dtype=np.float64)
-    p = np.asarray(p, dtype=np.float64)
-    xq, xc = X[qi], X[cj]
-    diff = xq[:, None, :] - xc[None, :, :]
-    d2 = np.sum(diff * diff, axis=2)
+    qi = np.asarray(qi, dtype=np.int64).reshape(-1)
+    cj = np.asarray(cj, dtype=np.int64).reshape(-1)
+    inv_ls = 1.0 / np.broadcast_to(np.asarray(ls, dtype=np.float64).reshape(-1), (coords.shape[1],))
+    xq = np.asarray(coords[qi], dtype=np.float64) * inv_ls
+    xc = np.asarray(coords[cj], dtype=np.float64) * inv_ls
+    # squared distance one axis at a time (no q x c x D temporary at large N)
+    d2 = np.zeros((qi.size, cj.size))
+    for a in range(xq.shape[1]):
+        t = xq[:, a][:, None] - xc[:, a][None, :]
+        t *= t
+        d2 += t
     if kernel_type == 1:
-        a = np.sqrt(5.0) * np.sqrt(d2)
-        K = var * (1.0 + a + a * a / 3.0) * np.exp(-a)
+        a_ = np.sqrt(d2)
+        a_ *= np.sqrt(5.0)
+        K = var * (1.0 + a_ + a_ * a_ / 3.0) * np.exp(-a_)
     else:
-        K = var * np.exp(-0.5 * d2)
-    dot = V[qi] @ V[cj].T
-    denom = np.sqrt(np.maximum(p[qi][:, None] * p[cj][None, :], 1e-18))
-    rho = np.clip((K - dot) / denom, -1.0, 1.0)
-    d = np.sqrt(np.maximum(1.0 - np.abs(rho), 0.0))
-    same = np.asarray(qi)[:, None] == np.asarray(cj)[None, :]
-    d[same] = 0.0
+        d2 *= -0.5
+        K = var * np.exp(d2)
+    K -= np.asarray(V[qi], dtype=np.float64) @ np.asarray(V[cj], dtype=np.float64).T
+    pq = np.asarray(p[qi], dtype=np.float64)
+    pc = np.asarray(p[cj], dtype=np.float64)
+    K /= np.sqrt(np.maximum(pq[:, None] * pc[None, :], 1e-18))
+    np.clip(K, -1.0, 1.0, out=K)
+    np.abs(K, out=K)
+    d = np.sqrt(np.maximum(1.0 - K, 0.0))
+    d[qi[:, None] == cj[None, :]] = 0.0
     return d
 
 
@@ -179,14 +192,20 @@ def brute_knn_f64(V, p, coords, var, ls, kernel_type, queries, k, predecessor, b
     queries = np.asarray(queries, dtype=np.int64)
     out_i = np.full((queries.size, k), -1, dtype=np.int64)
     out_d = np.full((queries.size, k), np.inf, dtype=np.float64)
-    allc = np.arange(n)
+    # blocks of queries close in id, so that predecessor mode only scores [0, max id)
+    order_q = np.argsort(queries, kind="stable")
     for s in range(0, queries.size, block):
-        qb = queries[s:s + block]
+        rows = order_q[s:s + block]
+        qb = queries[rows]
+        hi = n if not predecessor else int(min(n, max(int(qb.max()), 0)))
+        if hi <= 0:
+            continue
+        allc = np.arange(hi)
         D = residual_dist_f64(V, p, coords, var, ls, kernel_type, qb, allc)
         if predecessor:
             D[allc[None, :] >= qb[:, None]] = np.inf
-        kk = min(k, n)
-        part = np.argpartition(D, kk - 1, axis=1)[:, :kk] if kk < n else np.tile(allc, (qb.size, 1))
+        kk = min(k, hi)
+        part = np.argpartition(D, kk - 1, axis=1)[:, :kk] if kk < hi else np.tile(allc, (qb.size, 1))
         for r in range(qb.size):
             cand = part[r]
             # widen to include exact ties at the boundary, then lexsort (dist, idx)
@@ -195,9 +214,24 @@ def brute_knn_f64(V, p, coords, var, ls, kernel_type, queries, k, predecessor, b
             order = np.lexsort((cand, D[r, cand]))
             sel = cand[order][:k]
             sel = sel[np.isfinite(D[r, sel])]
-            out_i[s + r, :sel.size] = sel
-            out_d[s + r, :sel.size] = D[r, sel]
+            out_i[rows[r], :sel.size] = sel
+            out_d[rows[r], :sel.size] = D[r, sel]
     return out_i, out_d
+
+
+def brute_knn_f64_c(V, p, coords, var, ls, kernel_type, queries, k, predecessor, cand_limit=None, threads=0):
+    """The FP64 brute force of ``brute_knn_f64`` in C (OpenMP, query blocks sharing each
+    candidate row), for the full-size shapes; same formula, ordering and padding."""
+    L = lib()
+    V = _c(V, np.float32); p = _c(p, np.float32).reshape(-1); coords = _c(coords, np.float32)
+    ls = _c(np.atleast_1d(ls), np.float32)
+    q = _c(queries, np.int64).reshape(-1)
+    oi = np.empty((q.size, k), np.int64)
+    od = np.empty((q.size, k), np.float64)
+    L.ct_oracle_brute_f64(_p(V, _f32p), _p(p, _f32p), _p(coords, _f32p), V.shape[0], V.shape[1], coords.shape[1],
+                          float(var), _p(ls, _f32p), ls.size, int(kernel_type), _p(q, _i64p), q.size, int(k),
+                          int(predecessor), int(cand_limit or 0), _p(oi, _i64p), _p(od, _f64p), int(threads))
+    return oi, od
 
 
 # --------------------------------------------------------------------------
@@ -390,12 +424,21 @@ def brute_knn_euclidean_f64(points, queries, k, predecessor=False):
     out_d = np.full((Qp.shape[0], k), np.inf)
     for s in range(0, Qp.shape[0], 512):
         qb = Qp[s:s + 512]
-        D = np.sqrt(np.maximum(((qb[:, None, :] - P[None, :, :]) ** 2).sum(-1), 0))
+        D = np.zeros((qb.shape[0], n))
+        for a in range(P.shape[1]):
+            t = qb[:, a][:, None] - P[:, a][None, :]
+            t *= t
+            D += t
+        np.sqrt(D, out=D)
         if predecessor:
             rows = np.arange(s, s + qb.shape[0])
             D[np.arange(n)[None, :] >= rows[:, None]] = np.inf
+        kk = min(k, n)
+        part = np.argpartition(D, kk - 1, axis=1)[:, :kk] if kk < n else np.tile(np.arange(n), (qb.shape[0], 1))
         for r in range(qb.shape[0]):
-            order = np.lexsort((np.arange(n), D[r]))[:k]
+            # widen to the exact ties at the boundary, then order by (dist, idx)
+            cand = np.nonzero(D[r] <= D[r, part[r]].max())[0]
+            order = cand[np.lexsort((cand, D[r, cand]))][:k]
             order = order[np.isfinite(D[r, order])]
             out_i[s + r, :order.size] = order
             out_d[s + r, :order.size] = D[r, order]

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests._data import gaussian_case
+from tests._data import gaussian_case, mixture_case
 
 GOLD = __import__("pathlib").Path(__file__).resolve().parent / "golden"
 
@@ -239,3 +239,18 @@ def test_euclidean_oracle_restatement():
     assert recall > 0.95
     true_d = np.sqrt(((X[:, None, :].astype(np.float64) - X[oi].astype(np.float64)) ** 2).sum(-1))
     assert np.abs(od - true_d).max() < 1e-5
+
+
+@pytest.mark.parametrize("predecessor", [False, True])
+def test_fp64_brute_c_matches_numpy(predecessor):
+    """The blocked C FP64 brute force (used at the full benchmark shapes) returns the
+    numpy FP64 brute force's rows: same ids, distances within FP64 summation-order noise
+    (the inducing rows divide by sqrt(p_q p_c) ~ 1e-6, which scales that noise up)."""
+    case = mixture_case(3000, 8, 128, 2.0)
+    q = np.random.default_rng(7).choice(3000, 333, replace=False)
+    a_i, a_d = O.brute_knn_f64(case["V"], case["p"], case["X"], 1.0, case["ls"], 0, q, 30, predecessor)
+    b_i, b_d = O.brute_knn_f64_c(case["V"], case["p"], case["X"], 1.0, case["ls"], 0, q, 30, predecessor)
+    assert np.array_equal(a_i, b_i)
+    fin = np.isfinite(a_d)
+    assert np.array_equal(fin, np.isfinite(b_d))
+    assert np.abs(a_d[fin] - b_d[fin]).max() < 1e-9

@@ -11,6 +11,7 @@ import ctypes
 import numpy as np
 import pytest
 
+from oracle import oracle as O
 from tests._data import gaussian_case
 
 pytestmark = pytest.mark.gpu
@@ -62,6 +63,43 @@ def test_noalloc_matches_dense_entry_point_twice_in_a_row(cuda_available):
     # same kernel, same arithmetic: bit-exact (tolerance 0)
     assert np.array_equal(ia, ra_i) and np.array_equal(da.view(np.uint32), ra_d.view(np.uint32))
     assert np.array_equal(ib, rb_i) and np.array_equal(db.view(np.uint32), rb_d.view(np.uint32))
+    # and, independently of the dense entry point, bit-exact against the CPU oracle's
+    # f32 brute force (the reference's batch-path distance)
+    for case, q, k, pred, gi, gd in ((a, qa, 20, True, ia, da), (b, qb, 16, False, ib, db)):
+        oi, od = O.brute_knn_f32(case["V"], case["p"], case["X"], case["var"], case["ls"], case["kt"], q, k, pred)
+        assert np.array_equal(gi, oi) and np.array_equal(gd.view(np.uint32), od.view(np.uint32))
+
+
+def _bytes_needed(n, m, d):
+    """The documented scratch rule: five pieces, each rounded up to 256 bytes."""
+    a = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    return a(4 * n * m) + a(4 * n * d) + a(4 * n) + a(4 * n) + 256
+
+
+def test_noalloc_accepts_the_largest_input_and_rejects_one_row_more(cuda_available):
+    import torch
+
+    from covertreex_gb300 import _lib
+
+    L = _lib.load()
+    m, d = 64, 3
+    n = 243145
+    assert _bytes_needed(n, m, d) == _lib.CT_NOALLOC_SCRATCH_BYTES < _bytes_needed(n + 1, m, d)
+    r = np.random.default_rng(9)
+    case = {"V": (0.1 * r.standard_normal((n + 1, m))).astype(np.float32),
+            "p": r.uniform(0.05, 1.0, n + 1).astype(np.float32),
+            "X": r.standard_normal((n + 1, d)).astype(np.float32),
+            "ls": np.ones(d, np.float32), "var": 1.0, "kt": 0}
+    at_limit = {key: (val[:n] if key in ("V", "p", "X") else val) for key, val in case.items()}
+    q = r.choice(n, 64, replace=False)
+    stream = torch.cuda.current_stream()
+    rc, gi, gd = _noalloc(L, at_limit, q, 10, False, torch, stream)
+    assert rc == 0, L.ct_last_error()
+    ri, rd = _reference_call(at_limit, q, 10, False)
+    assert np.array_equal(gi, ri) and np.array_equal(gd.view(np.uint32), rd.view(np.uint32))
+    rc, _, _ = _noalloc(L, case, q, 10, False, torch, stream)
+    assert rc == _lib.CT_ERR_UNSUPPORTED
+    assert b"scratch" in L.ct_last_error()
 
 
 def test_noalloc_rejects_inputs_beyond_the_scratch(cuda_available):

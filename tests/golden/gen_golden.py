@@ -18,6 +18,10 @@ Outputs (small .npz files next to this script):
   hilbert.npz           _hilbert_permutation (order/strategy.py:38-100) permutations
   prefix.npz            prefix_slices (order/helpers.py:59-71)
   distance.npz          compute_distance_chunk (metrics/_residual_numba.py:148-221) distances
+  residual_knn.npz      _single_query_residual_knn (queries/residual_knn.py:249-386), the
+                        reference's Python residual kNN, on a flat tree (every point a root,
+                        so the best-first search visits every point): neighbour ids and
+                        distances for 4 small cases, with and without predecessor mode
 """
 from __future__ import annotations
 
@@ -169,6 +173,38 @@ def main(ref_root: str) -> None:
         dq, _ = resn.compute_distance_chunk(V[q], V, kern[q], float(p[q]), p, float(norms[q]), norms, 1.0, 1e-9)
         dist[q] = dq
     np.savez_compressed(OUT / "distance.npz", X=X, V=hb.v_matrix, p=hb.p_diag, dist=dist)
+
+    # ---- the reference's own residual kNN search (Python path), exhaustive on a flat tree
+    from covertreex.queries import residual_knn as rknn
+    from covertreex.queries.utils import ChildChainCache
+
+    knn = {}
+    for ci, (n, d, m, kt, ls, k, pred, seed) in enumerate([(400, 3, 32, 0, 1.0, 10, False, 31),
+                                                          (500, 2, 48, 1, 0.8, 16, True, 32),
+                                                          (300, 5, 64, 0, 2.0, 8, True, 33),
+                                                          (350, 3, 40, 1, 1.3, 12, False, 34)]):
+        X = np.random.default_rng(seed).standard_normal((n, d)).astype(np.float32)
+        hb = build_residual_backend(X, seed=42, inducing_count=m, variance=1.0, lengthscale=ls, kernel_type=kt)
+        flat_children = np.full(n, -1, np.int64)
+        cache = ChildChainCache(flat_children, np.full(n, -1, np.int64))
+        rows_i = np.full((n, k), -1, np.int64)
+        rows_d = np.full((n, k), np.inf)
+        for q in range(n):
+            kk = min(k, q) if pred else k
+            if kk <= 0:
+                continue
+            ids, dists = rknn._single_query_residual_knn(
+                q, tree_indices=np.arange(n, dtype=np.int64), si_cache=np.zeros(n), child_cache=cache,
+                root_indices=np.arange(n, dtype=np.int64), k=kk, host_backend=hb, predecessor_mode=pred)
+            rows_i[q, :len(ids)] = ids
+            rows_d[q, :len(ids)] = dists
+        knn[f"X{ci}"] = X
+        knn[f"V{ci}"] = hb.v_matrix
+        knn[f"p{ci}"] = hb.p_diag
+        knn[f"idx{ci}"] = rows_i
+        knn[f"dist{ci}"] = rows_d
+        knn[f"meta{ci}"] = np.array([kt, ls, k, int(pred)], dtype=np.float64)
+    np.savez_compressed(OUT / "residual_knn.npz", **knn)
     print("golden vectors written to", OUT)
 
 

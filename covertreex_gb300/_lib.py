@@ -67,6 +67,7 @@ EXPORTED_SYMBOLS = (
     "ct_batch_free",
     "ct_batch_order",
     "ct_luby_mis",
+    "ct_tree_build_info",
 )
 
 
@@ -181,6 +182,9 @@ def load(build_if_missing: bool = True):
         L.ct_batch_free.argtypes = [vp]
         L.ct_batch_order.restype = ctypes.c_int
         L.ct_batch_order.argtypes = [vp, i64, i32, i32, vp, vp]
+        L.ct_tree_build_info.restype = ctypes.c_int
+        L.ct_tree_build_info.argtypes = [vp, ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(i64),
+                                         ctypes.POINTER(i64), ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_double)]
         L.ct_luby_mis.restype = ctypes.c_int
         L.ct_luby_mis.argtypes = [vp, vp, i64, u64, vp, ip32, vp]
         _handle = L

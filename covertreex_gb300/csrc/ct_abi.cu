@@ -309,6 +309,19 @@ int ct_tree_device_bytes(const ct_tree* T, int64_t* bytes) {
     return CT_OK;
 }
 
+int ct_tree_build_info(const ct_tree* T, int64_t* groups, int64_t* conflict_edges, int64_t* selected,
+                       int64_t* side_rows, int64_t* roots, double* build_ms) {
+    if (!T) return fail(CT_ERR_ARG, "ct_tree_build_info: tree is NULL");
+    if (!T->has_tree) return fail(CT_ERR_STATE, "ct_tree_build_info: tree was built with CT_BUILD_METRIC_ONLY");
+    if (groups) *groups = T->build_groups;
+    if (conflict_edges) *conflict_edges = T->build_conflict_edges;
+    if (selected) *selected = T->build_selected;
+    if (side_rows) *side_rows = T->n_side;
+    if (roots) *roots = T->n_roots;
+    if (build_ms) *build_ms = T->build_ms;
+    return CT_OK;
+}
+
 int ct_tree_shape(const ct_tree* T, int64_t* n, int32_t* m, int32_t* d) {
     if (!T) return fail(CT_ERR_ARG, "ct_tree_shape: tree is NULL");
     if (n) *n = T->n;

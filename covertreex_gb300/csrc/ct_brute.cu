@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kThreads, 1) brute_knn_kernel(BruteParams P) {
     J.nq = P.nq;
     // heavy tiles (large query ids in predecessor mode) first
     J.q0 = ((long long)gridDim.x - 1 - blockIdx.x) * QT;
-    J.cbeg = 0; J.cend = P.n;
+    J.cbeg = P.cbeg; J.cend = P.cend > 0 ? P.cend : P.n;
     J.out_idx = P.out_idx; J.out_dist = P.out_dist; J.out_stride = P.k;
     dense::run_tile<QT>(J, smem_raw);
 }

@@ -1,33 +1,41 @@
-// ct_build.cu — device cover-tree build (the batch build of the reference's
-// build_pcct2_residual_tree, src/lib.rs:1374-1564, and of the Python PCCT path,
-// covertreex/algo/batch/insert.py:43-803), re-designed level-synchronous for a GPU.
+// ct_build.cu — device cover-tree build: the batch insert of the reference's
+// PCCT path (prefix-doubling groups, covertreex/algo/batch/insert.py:671-803 with
+// prefix_slices, algo/order/helpers.py:59-71; traversal level and parent, conflict
+// graph, MIS, selected / dominated insertion, insert.py:43-640) and of its Rust
+// build_pcct2_residual_tree (far-set conflicts at radius 2^l, MIS, leaders and
+// attached non-leaders, src/algo/batch/mod.rs:447-999), re-designed for one GPU.
 //
-//  1. Batch order: Hilbert keys + LSD radix sort (ct_order.cu); node i of the
-//     tree is the point at sorted position i, and V / coordinates are copied
-//     into that order so subtrees are contiguous in memory.
-//  2. Coarsening, finest radius first.  The active set S starts as all nodes.
-//     At radius r (2^-9, 2^-8, ..., 1, then 1 again until |S| <= 64):
-//       * conflict graph: an edge joins two active nodes within kWindow positions
-//         of each other (in S's Hilbert order) whose residual distance is <= r;
-//       * seeded Luby MIS on that graph with warp ballots (hash priorities of
-//         covertreex/algo/_mis_numba.py:19-28, lower index wins ties); a
-//         maximal independent set keeps every non-selected node next to a
-//         selected one;
-//       * every non-selected node attaches to its nearest selected neighbour
-//         (its parent; its level is log2 r); the selected nodes form the next S.
-//     The nodes left at the end are the roots.
-//  3. Cover radii: si[a] = max over descendants x of d(a, x), computed exactly
-//     by walking each node's ancestor chain (the reference's
-//     compute_si_cache_residual, src/algo.rs:52-106, stores the looser
-//     sum d(node, child) + si[child]); subtree_min[a] = min dataset id below a
-//     (compute_subtree_index_bounds, src/tree.rs:144-185).
-//  4. Children in CSR (child_off / child_idx), roots listed separately.
+//  1. Node order: Hilbert keys + LSD radix sort (ct_order.cu).  Rows whose residual
+//     variance is tiny (p < 1/kSideIsp^2: the inducing rows, p ~ 1e-6) are moved to
+//     the end and kept out of the tree: their distances carry errors of order 1 in
+//     FP32 and no cover radius could prune a subtree holding one; every query scores
+//     them directly (they are roots without children, like the reference's dropped
+//     points).  The first remaining node is the root, at level 0 (radius 2^0 = 1
+//     covers every residual distance).
+//  2. Prefix doubling: the other nodes are inserted in groups [1,2), [2,4), [4,8), ...
+//     (prefix_slices).  For a group G inserted into the tree T built so far:
+//       * traversal: each x in G finds its nearest node t(x) in T (dense exact FP32
+//         search, ct_dense.cuh) and the level l(x) = min(ceil(log2 d) - 1, level(t) - 1),
+//         so that d(x, t) <= 2^(l+1) whenever the parent's level allows it;
+//       * conflict graph: x and y in G conflict when d(x, y) <= 2^min(l(x), l(y)); the
+//         candidate pairs are each point's kConflictK nearest group members (the degree
+//         cap of the reference's conflict_degree_cap), made symmetric without duplicates;
+//       * seeded Luby MIS on the device (ct_mis.cu, the reference's _mis_numba rules);
+//       * selected points join at level l(x) under t(x); every dominated point joins
+//         under its nearest selected neighbour at level min(l(x) - 1, level(parent) - 1,
+//         floor(log2 d)) (insert.py:586-640).
+//  3. Radii: si[a] = max over descendants x of the FP32 distance d(a, x) (exact, by
+//     walking every node's ancestor chain); si_up[a] = max of a certified upper bound
+//     of the ideal metric's d(a, x) (the FP32 value plus its error bound, see
+//     ct_traverse.cu); sub_isp[a] = max over the subtree of 1/sqrt(p); subtree_min[a]
+//     = min dataset id below a (compute_subtree_index_bounds, src/tree.rs:144-185).
+//  4. Children in CSR (child_off / child_idx); roots (the root and the side rows).
 //
-// Distances use the reference's batch-path f32 arithmetic (the same device
-// functions as the dense form), evaluated by half-warps: lane l of a half owns
-// the accumulator of elements 16c + l, so a pair's value is bit-identical to
-// the dense form's.
+// Distances use the reference's batch-path f32 arithmetic (the dense form's device
+// functions), so every distance the build evaluates is bit-identical to the one the
+// dense form and the traversal evaluate for the same pair.
 #include <climits>
+#include <cmath>
 
 #include <algorithm>
 #include <vector>
@@ -35,12 +43,14 @@
 #include "ct_common.cuh"
 #include "ct_internal.h"
 #include "ct_tree.h"
+#include "ct_treebound.cuh"
 
 namespace ct {
 namespace treeb {
 
-constexpr int kWindow = 32;  // neighbours on each side in the active order
-constexpr int kMaxRoots = 64;
+constexpr int kLevelTop = 0;
+constexpr int kLevelMin = -30;
+constexpr int kConflictK = 16;
 
 struct TreeData {
     const float* v;    // n x m natural layout, node order
@@ -75,148 +85,146 @@ __device__ __forceinline__ float half_dist(const TreeData& T, int a, int b) {
     return residual_from_parts(kv, dot, T.p[a], T.p[b]);
 }
 
-__device__ __forceinline__ double hash_priority(unsigned node, unsigned seed, unsigned iteration) {
-    unsigned x = node ^ seed;
-    x ^= (unsigned)((unsigned long long)iteration * 0x9E3779B9ULL);
-    x ^= x << 13;
-    x ^= x >> 17;
-    x ^= x << 5;
-    return ((double)x + 1.0) / 4294967296.0;
+// Smallest L with d <= 2^L (d > 0), as an integer; kLevelMin + 1 for d == 0.
+__device__ __forceinline__ int ceil_log2(float d) {
+    if (!(d > 0.f)) return kLevelMin + 1;
+    int e;
+    const float f = frexpf(d, &e);  // d = f 2^e, f in [0.5, 1)
+    return f == 0.5f ? e - 1 : e;
+}
+// Largest L with 2^L <= d (d > 0); kLevelMin for d == 0.
+__device__ __forceinline__ int floor_log2(float d) {
+    if (!(d > 0.f)) return kLevelMin;
+    int e;
+    frexpf(d, &e);
+    return e - 1;
 }
 
-// adjacency: bit w of mask[i] <-> neighbour at active position i + (w - kWindow) (w != kWindow)
-__global__ void conflict_edges_kernel(TreeData T, const int* __restrict__ act, int na, float r,
-                                      unsigned long long* __restrict__ mask) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int half = (threadIdx.x >> 4) & 1;
-    const int lane16 = threadIdx.x & 15;
-    if (warp >= na) return;
-    const int i = warp;
-    unsigned long long bits = 0;
-    for (int w = half; w < 2 * kWindow + 1; w += 2) {
-        const int j = i + w - kWindow;
-        if (w == kWindow || j < 0 || j >= na) continue;
-        const float dd = half_dist(T, act[i], act[j]);
-        if (dd <= r) bits |= 1ULL << w;
-    }
-    // combine the two halves' bits
-    bits |= __shfl_xor_sync(0xffffffffu, bits, 16);
-    if ((threadIdx.x & 31) == 0) mask[i] = bits;
-    (void)lane16;
+// Traversal level of the group's points: t[i] = nearest tree node, td[i] its distance.
+__global__ void group_level_kernel(long long s, long long g, const long long* __restrict__ t,
+                                   const float* __restrict__ td, const int* __restrict__ levels,
+                                   int* __restrict__ lvl) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g) return;
+    const long long pnt = t[i];
+    const int pl = pnt >= 0 ? levels[pnt] : kLevelTop;
+    int l = ceil_log2(td[i]) - 1;
+    if (l > pl - 1) l = pl - 1;
+    if (l < kLevelMin) l = kLevelMin;
+    lvl[i] = l;
 }
 
-// One Luby round: an active node wins if no active neighbour has a higher
-// (priority, lower index) rank.  A warp handles 32 nodes; lanes test their
-// node's neighbours and the warp ballots on the outcome.
-__global__ void luby_round_kernel(const unsigned long long* __restrict__ mask, int na, unsigned seed, unsigned round,
-                                  unsigned char* __restrict__ state, int* __restrict__ any_active) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool win = false;
-    if (i < na && state[i] == 0) {
-        const double pi = hash_priority((unsigned)i, seed, round);
-        win = true;
-        unsigned long long b = mask[i];
-        while (b) {
-            const int w = __ffsll((long long)b) - 1;
-            b &= b - 1;
-            const int j = i + w - kWindow;
-            if (state[j] != 0 && state[j] != 3) continue;  // 3 = winning this round, still active
-            const double pj = hash_priority((unsigned)j, seed, round);
-            if (pj > pi || (pj == pi && j < i)) { win = false; break; }
+__device__ __forceinline__ bool lists_member(const long long* __restrict__ cidx, int kc, long long row, long long x) {
+    for (int j = 0; j < kc; ++j)
+        if (cidx[row * kc + j] == x) return true;
+    return false;
+}
+
+// Conflict edges from the group's kNN lists (node ids): x -- y when y is among x's
+// nearest group members and d(x, y) <= 2^min(l(x), l(y)).  x's row always gets y;
+// y's row gets x only when x is not on y's own list (y adds it itself otherwise), so
+// no edge is stored twice.  pass 0 counts, pass 1 fills (with the distances).
+__global__ void conflict_edges_kernel(long long s, long long g, const long long* __restrict__ cidx,
+                                      const float* __restrict__ cd, int kc, const int* __restrict__ lvl,
+                                      int pass, int* __restrict__ deg, int* __restrict__ cursor,
+                                      long long* __restrict__ indices, float* __restrict__ w) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g) return;
+    const long long x = s + i;
+    for (int j = 0; j < kc; ++j) {
+        const long long y = cidx[i * kc + j];
+        if (y < s || y >= s + g || y == x) continue;
+        const long long yi = y - s;
+        const int l = min(lvl[i], lvl[yi]);
+        const float dd = cd[i * kc + j];
+        if (!(dd <= ldexpf(1.f, l))) continue;
+        const bool reverse = !lists_member(cidx, kc, yi, x);
+        if (pass == 0) {
+            atomicAdd(&deg[i], 1);
+            if (reverse) atomicAdd(&deg[yi], 1);
+        } else {
+            const int a = atomicAdd(&cursor[i], 1);
+            indices[a] = yi;
+            w[a] = dd;
+            if (reverse) {
+                const int b = atomicAdd(&cursor[yi], 1);
+                indices[b] = i;
+                w[b] = dd;
+            }
         }
     }
-    const unsigned wins = __ballot_sync(0xffffffffu, win);
-    if (win) state[i] = 3;  // tentatively selected this round
-    if ((threadIdx.x & 31) == 0 && wins) atomicOr(any_active, 1);
 }
 
-// Commit a round: winners become selected (1), their neighbours excluded (2).
-__global__ void luby_commit_kernel(const unsigned long long* __restrict__ mask, int na,
-                                   unsigned char* __restrict__ state, int* __restrict__ remaining) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= na) return;
-    if (state[i] == 3) { state[i] = 1; return; }
-    if (state[i] != 0) return;
-    unsigned long long b = mask[i];
-    while (b) {
-        const int w = __ffsll((long long)b) - 1;
-        b &= b - 1;
-        const int j = i + w - kWindow;
-        if (state[j] == 3 || state[j] == 1) { state[i] = 2; return; }
+// Selected points join under their traversal parent; dominated points under their
+// nearest selected neighbour (ties to the lower node), one level below it at most.
+__global__ void group_assign_kernel(long long s, long long g, const signed char* __restrict__ sel,
+                                    const long long* __restrict__ indptr, const long long* __restrict__ indices,
+                                    const float* __restrict__ w, const long long* __restrict__ t,
+                                    const int* __restrict__ lvl, long long* __restrict__ parents,
+                                    int* __restrict__ levels, int* __restrict__ selected_count) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= g) return;
+    const long long x = s + i;
+    if (sel[i]) {
+        parents[x] = t[i];
+        levels[x] = lvl[i];
+        atomicAdd(selected_count, 1);
+        return;
     }
-    atomicAdd(remaining, 1);
-}
-
-// Non-selected nodes attach to their nearest selected neighbour (one warp per node).
-__global__ void attach_kernel(TreeData T, const int* __restrict__ act, int na, const unsigned long long* __restrict__ mask,
-                              const unsigned char* __restrict__ state, int level, long long* __restrict__ parents,
-                              int* __restrict__ levels) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int half = (threadIdx.x >> 4) & 1;
-    if (warp >= na) return;
-    const int i = warp;
-    if (state[i] != 2) return;  // selected (or undecided, kept as selected) nodes do not attach
     float best = CT_FLT_MAX;
-    int bj = -1;
-    for (int w = half; w < 2 * kWindow + 1; w += 2) {
-        const int j = i + w - kWindow;
-        if (!((mask[i] >> w) & 1ULL) || state[j] != 1) continue;
-        const float dd = half_dist(T, act[i], act[j]);
-        if (dd < best || (dd == best && j < bj)) { best = dd; bj = j; }
+    long long bj = -1;
+    for (long long o = indptr[i]; o < indptr[i + 1]; ++o) {
+        const long long j = indices[o];
+        if (!sel[j]) continue;
+        if (w[o] < best || (w[o] == best && j < bj)) { best = w[o]; bj = j; }
     }
-    const float ob = __shfl_xor_sync(0xffffffffu, best, 16);
-    const int oj = __shfl_xor_sync(0xffffffffu, bj, 16);
-    if (oj >= 0 && (ob < best || (ob == best && (bj < 0 || oj < bj)))) { best = ob; bj = oj; }
-    if ((threadIdx.x & 31) == 0 && bj >= 0) {
-        parents[act[i]] = act[bj];
-        levels[act[i]] = level;
+    if (bj < 0) {  // cannot happen for a maximal independent set; keep the traversal parent
+        parents[x] = t[i];
+        levels[x] = lvl[i];
+        return;
     }
+    int l = lvl[i] - 1;
+    l = min(l, lvl[bj] - 1);
+    l = min(l, floor_log2(best));
+    if (l < kLevelMin) l = kLevelMin;
+    parents[x] = s + bj;
+    levels[x] = l;
 }
 
-// Stream compaction of the selected nodes (one block; order preserved).
-__global__ void __launch_bounds__(1024) compact_selected_kernel(const int* __restrict__ act, int na,
-                                                                const unsigned char* __restrict__ state,
-                                                                int* __restrict__ out, int* __restrict__ nout) {
-    // selected (1) and, should the round limit ever be hit, undecided (0) nodes
-    __shared__ int warp_tot[32];
-    __shared__ int base;
-    if (threadIdx.x == 0) base = 0;
-    __syncthreads();
-    for (int c0 = 0; c0 < na; c0 += 1024) {
-        const int i = c0 + threadIdx.x;
-        const bool sel = i < na && (state[i] == 1 || state[i] == 0);  // undecided nodes stay active
-        const unsigned bal = __ballot_sync(0xffffffffu, sel);
-        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-        if (lane == 0) warp_tot[wid] = __popc(bal);
-        __syncthreads();
-        int before = 0;
-        for (int w = 0; w < wid; ++w) before += warp_tot[w];
-        if (sel) out[base + before + __popc(bal & ((1u << lane) - 1u))] = act[i];
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int t = 0;
-            for (int w = 0; w < 32; ++w) t += warp_tot[w];
-            base += t;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *nout = base;
+// Per node: 1/sqrt(p) rounded up and ||v|| rounded up (inputs of the certified bounds).
+__global__ void node_scalars_kernel(TreeData T, long long n, float* __restrict__ isp, float* __restrict__ vn) {
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    const float* v = T.v + (size_t)r * T.m;
+    double s = 0.0;
+    for (int c = 0; c < T.m; ++c) s += (double)v[c] * (double)v[c];
+    vn[r] = (float)(sqrt(s) * (1.0 + 1e-6));
+    const double pr = (double)T.p[r];
+    isp[r] = pr > 0.0 ? (float)(1.0 / sqrt(pr) * (1.0 + 1e-6)) : 3.0e38f;
 }
 
-// si and subtree_min by walking every node's ancestor chain (one half-warp per node).
-__global__ void ancestors_kernel(TreeData T, int n, const long long* __restrict__ parents,
-                                 const long long* __restrict__ order, unsigned* __restrict__ si_bits,
+// si, si_up, subtree_min and sub_isp by walking every node's ancestor chain (one
+// half-warp per node); atomicMax on the bits of non-negative floats orders them.
+__global__ void ancestors_kernel(TreeData T, BoundModel B, int n, const long long* __restrict__ parents,
+                                 const long long* __restrict__ order, const float* __restrict__ isp,
+                                 const float* __restrict__ vn, unsigned* __restrict__ si_bits,
+                                 unsigned* __restrict__ si_up_bits, unsigned* __restrict__ sub_isp_bits,
                                  long long* __restrict__ sub_min) {
     const int hw = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
     if (hw >= n) return;
     const int x = hw;
     const long long ds = order[x];
+    const float ispx = isp[x];
     long long a = parents[x];
     int guard = 0;
     while (a >= 0 && guard < 4096) {
         const float dd = half_dist(T, (int)a, x);
         if ((threadIdx.x & 15) == 0) {
+            const float delta = pair_delta(B, T.norms[a], T.norms[x], vn[a], vn[x], isp[a], ispx);
+            const float up = dist_upper(dd, delta);
             atomicMax(&si_bits[a], __float_as_uint(dd));
+            atomicMax(&si_up_bits[a], __float_as_uint(up));
+            atomicMax(&sub_isp_bits[a], __float_as_uint(ispx));
             atomicMin((unsigned long long*)&sub_min[a], (unsigned long long)ds);
         }
         a = parents[a];
@@ -224,15 +232,17 @@ __global__ void ancestors_kernel(TreeData T, int n, const long long* __restrict_
     }
 }
 
-__global__ void init_tree_kernel(int n, long long* parents, int* levels, unsigned* si_bits, long long* sub_min,
-                                 const long long* order, int* act) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void init_tree_kernel(long long n, long long* parents, int* levels, unsigned* si_bits,
+                                 unsigned* si_up_bits, unsigned* sub_isp_bits, const float* isp, long long* sub_min,
+                                 const long long* order) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
     parents[i] = -1;
     levels[i] = INT_MIN;
     si_bits[i] = 0u;
+    si_up_bits[i] = 0u;
+    sub_isp_bits[i] = __float_as_uint(isp[i]);
     sub_min[i] = order[i];
-    act[i] = i;
 }
 
 __global__ void gather_rows_kernel(const float* __restrict__ src, const long long* __restrict__ order, long long n,
@@ -244,14 +254,24 @@ __global__ void gather_rows_kernel(const float* __restrict__ src, const long lon
     }
 }
 
-__global__ void to_i64_kernel(const int* in, long long n, long long* out) {
+__global__ void iota_kernel(long long s, long long g, long long* out) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i < n) out[i] = in[i];
+    if (i < g) out[i] = s + i;
 }
 
 __global__ void inverse_kernel(const long long* order, long long n, long long* inv) {
     const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i < n) inv[order[i]] = i;
+}
+
+__global__ void widen_kernel(const int* in, long long n, long long* out) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i];
+}
+
+__global__ void set_root_kernel(long long* parents, int* levels) {
+    parents[0] = -1;
+    levels[0] = kLevelTop;
 }
 
 }  // namespace treeb
@@ -266,104 +286,199 @@ int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_datase
     cudaError_t e = cudaSuccess;
     auto A = [&](void** ptr, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(ptr, bytes ? bytes : 16); };
     A((void**)&order, 8 * N); A((void**)&inv, 8 * N); A((void**)&parents, 8 * N); A((void**)&levels, 4 * N);
-    A((void**)&si, 4 * N); A((void**)&sub_min, 8 * N); A((void**)&child_off, 8 * (N + 1)); A((void**)&child_idx, 8 * N);
-    A((void**)&roots, 8 * kMaxRoots * 64);
+    A((void**)&si, 4 * N); A((void**)&si_up, 4 * N); A((void**)&sub_isp, 4 * N); A((void**)&sub_min, 8 * N);
+    A((void**)&child_off, 8 * (N + 1)); A((void**)&child_idx, 8 * N); A((void**)&roots, 8 * N);
     A((void**)&tvnat, sizeof(float) * N * m); A((void**)&txs, sizeof(float) * N * d);
     A((void**)&tnorms, sizeof(float) * N); A((void**)&tp, sizeof(float) * N);
-    int *order32 = nullptr, *act = nullptr, *act2 = nullptr, *counters = nullptr;
-    unsigned long long* mask = nullptr;
-    unsigned char* state = nullptr;
-    A((void**)&order32, 4 * N); A((void**)&act, 4 * N); A((void**)&act2, 4 * N); A((void**)&counters, 16);
-    A((void**)&mask, 8 * N); A((void**)&state, N);
+    A((void**)&tisp, sizeof(float) * N); A((void**)&tvn, sizeof(float) * N);
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "tree build allocation: %s", cudaGetErrorString(e));
 
-    // 1. batch order
-    if (order_mode == CT_ORDER_NATURAL) {
-        std::vector<int> id(N);
-        for (long long i = 0; i < N; ++i) id[i] = (int)i;
-        e = cudaMemcpyAsync(order32, id.data(), 4 * N, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    } else {
-        e = ct::compute_order(coords_raw, N, d, (d == 3 && order_mode == 2) ? 2 : 1, order32, st);
-    }
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    cudaEventRecord(ev0, st);
+
+    // 1. node order: Hilbert (or natural), then rows with tiny p moved to the end
+    int* order32 = nullptr;
+    A((void**)&order32, 4 * N);
     if (e == cudaSuccess) {
-        to_i64_kernel<<<gridn(N, 256), 256, 0, st>>>(order32, N, order);
+        if (order_mode == CT_ORDER_NATURAL) {
+            std::vector<int> id(N);
+            for (long long i = 0; i < N; ++i) id[i] = (int)i;
+            e = cudaMemcpyAsync(order32, id.data(), 4 * N, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        } else {
+            e = ct::compute_order(coords_raw, N, d, (d == 3 && order_mode == CT_ORDER_MORTON) ? 2 : 1, order32, st);
+        }
+    }
+    std::vector<int> ord(N);
+    std::vector<float> ph(N);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ord.data(), order32, 4 * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ph.data(), p, 4 * N, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    std::vector<long long> ord64;
+    n_side = 0;
+    if (e == cudaSuccess) {
+        ord64.reserve(N);
+        const float pside = 1.f / (ct::kSideIsp * ct::kSideIsp);
+        for (long long i = 0; i < N; ++i) if (!(ph[ord[i]] < pside)) ord64.push_back(ord[i]);
+        const long long n_tree = (long long)ord64.size();
+        for (long long i = 0; i < N; ++i) if (ph[ord[i]] < pside) ord64.push_back(ord[i]);
+        n_side = N - n_tree;
+        e = cudaMemcpyAsync(order, ord64.data(), 8 * N, cudaMemcpyHostToDevice, st);
+    }
+    cudaFree(order32);
+    const long long n_tree = N - n_side;
+    if (e == cudaSuccess) {
         inverse_kernel<<<gridn(N, 256), 256, 0, st>>>(order, N, inv);
-        // node-order copies (natural-layout V for the half-warp distances)
         gather_rows_kernel<<<152 * 8, 256, 0, st>>>(vnat, order, N, m, tvnat);
         gather_rows_kernel<<<152 * 8, 256, 0, st>>>(xs, order, N, d, txs);
         gather_rows_kernel<<<gridn(N, 256), 256, 0, st>>>(norms, order, N, 1, tnorms);
         gather_rows_kernel<<<gridn(N, 256), 256, 0, st>>>(p, order, N, 1, tp);
-        init_tree_kernel<<<gridn(N, 256), 256, 0, st>>>((int)N, parents, levels, (unsigned*)si, sub_min, order, act);
         e = cudaGetLastError();
     }
     TreeData TD{tvnat, txs, tnorms, tp, m, d, kernel_type, var};
-    // 2. coarsening
-    long long na = N;
-    int level = -9;
-    int guard = 0;
-    unsigned mis_seed = (unsigned)(seed & 0xffffffffu);
-    while (e == cudaSuccess && na > kMaxRoots && guard < 64) {
-        ++guard;
-        const float r = ldexpf(1.0f, level < 0 ? level : 0);
-        conflict_edges_kernel<<<gridn(na * 32, 256), 256, 0, st>>>(TD, act, (int)na, r, mask);
-        e = cudaMemsetAsync(state, 0, na, st);
-        int rounds = 0;
-        while (e == cudaSuccess && rounds < 256) {
-            ++rounds;
-            e = cudaMemsetAsync(counters, 0, 16, st);
-            if (e != cudaSuccess) break;
-            luby_round_kernel<<<gridn(na, 256), 256, 0, st>>>(mask, (int)na, mis_seed, (unsigned)rounds, state, counters);
-            luby_commit_kernel<<<gridn(na, 256), 256, 0, st>>>(mask, (int)na, state, counters + 1);
-            int h[2] = {0, 0};
-            e = cudaMemcpyAsync(h, counters, 8, cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            if (h[1] == 0) break;  // no undecided node left
-        }
-        if (e != cudaSuccess) break;
-        attach_kernel<<<gridn(na * 32, 256), 256, 0, st>>>(TD, act, (int)na, mask, state, level, parents, levels);
-        compact_selected_kernel<<<1, 1024, 0, st>>>(act, (int)na, state, act2, counters + 2);
-        int nn = 0;
-        e = cudaMemcpyAsync(&nn, counters + 2, 4, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) break;
-        std::swap(act, act2);
-        if (nn == na) {  // no progress at this radius: widen (radius capped at 1)
-            if (level >= 0) break;
-        }
-        na = nn;
-        if (level < 0) ++level;
-    }
-    // roots
-    std::vector<int> rootsv(na > 0 ? na : 0);
-    if (e == cudaSuccess && na > 0) e = cudaMemcpyAsync(rootsv.data(), act, 4 * na, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    n_roots = na;
-    std::vector<long long> rl(rootsv.begin(), rootsv.end());
-    if (e == cudaSuccess && na > 0) {
-        if (na > kMaxRoots * 64) return set_err(CT_ERR_STATE, "tree build left %lld roots", (long long)na);
-        e = cudaMemcpyAsync(roots, rl.data(), 8 * na, cudaMemcpyHostToDevice, st);
-    }
-    // 3. radii and subtree bounds
     if (e == cudaSuccess) {
-        ancestors_kernel<<<gridn(N * 16, 256), 256, 0, st>>>(TD, (int)N, parents, order, (unsigned*)si, sub_min);
+        node_scalars_kernel<<<gridn(N, 256), 256, 0, st>>>(TD, N, tisp, tvn);
+        init_tree_kernel<<<gridn(N, 256), 256, 0, st>>>(N, parents, levels, (unsigned*)si, (unsigned*)si_up,
+                                                        (unsigned*)sub_isp, tisp, sub_min, order);
         e = cudaGetLastError();
     }
-    // 4. children CSR (host assembles: n parents is a few MB)
+    // bound model of the tree: dataset maxima of ||v|| and of the scaled norms
+    if (e == cudaSuccess) {
+        std::vector<float> hv(N), hn(N);
+        e = cudaMemcpyAsync(hv.data(), tvn, 4 * N, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hn.data(), tnorms, 4 * N, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        float vmax = 0.f, nmax = 0.f;
+        for (long long i = 0; i < N; ++i) { vmax = std::max(vmax, hv[i]); nmax = std::max(nmax, hn[i]); }
+        bound = ct::make_bound_model(m, d, kernel_type, var, vmax, nmax);
+    }
+
+    // node-order residue-major V for the dense searches of the build (freed at the end)
+    float* tvperm = nullptr;
+    A((void**)&tvperm, sizeof(float) * N * m);
+    if (e == cudaSuccess) {
+        gather_rows_kernel<<<152 * 8, 256, 0, st>>>(vperm, order, N, m, tvperm);
+        e = cudaGetLastError();
+    }
+
+    // 2. prefix-doubling groups over nodes [1, n_tree)
+    build_groups = 0;
+    build_conflict_edges = 0;
+    build_selected = 0;
+    long long gmax = n_tree > 1 ? (n_tree - 1 + 1) / 2 + 1 : 1;
+    long long *gq = nullptr, *t_idx = nullptr, *c_idx = nullptr, *indptr = nullptr, *indices = nullptr;
+    float *t_d = nullptr, *c_d = nullptr, *w = nullptr;
+    int *lvl = nullptr, *deg = nullptr, *cursor = nullptr, *counters = nullptr;
+    signed char* sel = nullptr;
+    const int kc = (int)std::min<long long>(kConflictK + 1, std::max<long long>(gmax, 1));
+    A((void**)&gq, 8 * gmax); A((void**)&t_idx, 8 * gmax); A((void**)&t_d, 4 * gmax);
+    A((void**)&c_idx, 8 * gmax * kc); A((void**)&c_d, 4 * gmax * kc);
+    A((void**)&lvl, 4 * gmax); A((void**)&deg, 4 * (gmax + 1)); A((void**)&cursor, 4 * (gmax + 1));
+    A((void**)&indptr, 8 * (gmax + 1)); A((void**)&indices, 8 * gmax * 2 * kc); A((void**)&w, 4 * gmax * 2 * kc);
+    A((void**)&sel, gmax); A((void**)&counters, 16);
+    int smem_optin = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess && n_tree > 0) {
+        set_root_kernel<<<1, 1, 0, st>>>(parents, levels);
+        e = cudaGetLastError();
+    }
+    ct::BruteParams BP;
+    BP.vperm = tvperm; BP.xs = txs; BP.norms = tnorms; BP.p = tp; BP.n = N; BP.m = m; BP.d = d;
+    BP.kernel_type = kernel_type; BP.predecessor = 0; BP.var = var;
+    long long s = 1, size = 1;
+    while (e == cudaSuccess && s < n_tree) {
+        const long long g = std::min(size, n_tree - s);
+        ++build_groups;
+        iota_kernel<<<gridn(g, 256), 256, 0, st>>>(s, g, gq);
+        // traversal: nearest node of the tree built so far, nodes [0, s)
+        BP.qids = gq; BP.nq = g; BP.k = 1; BP.cbeg = 0; BP.cend = s; BP.out_idx = t_idx; BP.out_dist = t_d;
+        int qt = ct::brute_pick_qt(m, d, 1, (size_t)smem_optin);
+        if (qt == 0) { e = cudaErrorInvalidValue; break; }
+        e = ct::launch_brute_knn(BP, qt, st);
+        if (e != cudaSuccess) break;
+        group_level_kernel<<<gridn(g, 256), 256, 0, st>>>(s, g, t_idx, t_d, levels, lvl);
+        // conflict candidates: nearest group members (the point itself among them)
+        const int kk = (int)std::min<long long>(kc, g);
+        BP.k = kk; BP.cbeg = s; BP.cend = s + g; BP.out_idx = c_idx; BP.out_dist = c_d;
+        qt = ct::brute_pick_qt(m, d, kk, (size_t)smem_optin);
+        if (qt == 0) { e = cudaErrorInvalidValue; break; }
+        e = ct::launch_brute_knn(BP, qt, st);
+        if (e != cudaSuccess) break;
+        e = cudaMemsetAsync(deg, 0, 4 * (g + 1), st);
+        if (e != cudaSuccess) break;
+        conflict_edges_kernel<<<gridn(g, 256), 256, 0, st>>>(s, g, c_idx, c_d, kk, lvl, 0, deg, nullptr, nullptr,
+                                                             nullptr);
+        // exclusive scan of the degrees into indptr (g + 1 entries; g <= 2^30)
+        std::vector<int> hdeg(g + 1);
+        e = cudaMemcpyAsync(hdeg.data(), deg, 4 * g, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) break;
+        std::vector<long long> hptr(g + 1, 0);
+        std::vector<int> hcur(g);
+        for (long long i = 0; i < g; ++i) { hptr[i + 1] = hptr[i] + hdeg[i]; hcur[i] = (int)hptr[i]; }
+        build_conflict_edges += hptr[g];
+        e = cudaMemcpyAsync(indptr, hptr.data(), 8 * (g + 1), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(cursor, hcur.data(), 4 * g, cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) break;
+        conflict_edges_kernel<<<gridn(g, 256), 256, 0, st>>>(s, g, c_idx, c_d, kk, lvl, 1, nullptr, cursor, indices,
+                                                             w);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) break;
+        int iters = 0;
+        e = ct::luby_mis_csr(indptr, indices, g, (unsigned long long)(seed + (unsigned long long)build_groups), sel,
+                             &iters, st);
+        if (e != cudaSuccess) break;
+        e = cudaMemsetAsync(counters, 0, 16, st);
+        if (e != cudaSuccess) break;
+        group_assign_kernel<<<gridn(g, 256), 256, 0, st>>>(s, g, sel, indptr, indices, w, t_idx, lvl, parents, levels,
+                                                           counters);
+        int hs = 0;
+        e = cudaMemcpyAsync(&hs, counters, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // keeps the host vectors alive until copied
+        build_selected += hs;
+        s += g;
+        size = std::min(2 * size, n_tree - s);
+        if (size <= 0) size = 1;
+    }
+    cudaFree(gq); cudaFree(t_idx); cudaFree(t_d); cudaFree(c_idx); cudaFree(c_d); cudaFree(lvl); cudaFree(deg);
+    cudaFree(cursor); cudaFree(indptr); cudaFree(indices); cudaFree(w); cudaFree(sel); cudaFree(counters);
+    cudaFree(tvperm);
+
+    // 3. radii and subtree bounds
+    if (e == cudaSuccess) {
+        ancestors_kernel<<<gridn(N * 16, 256), 256, 0, st>>>(TD, bound, (int)N, parents, order, tisp, tvn,
+                                                             (unsigned*)si, (unsigned*)si_up, (unsigned*)sub_isp,
+                                                             sub_min);
+        e = cudaGetLastError();
+    }
+    // 4. children CSR and roots (host assembles: n parents is a few MB)
     std::vector<long long> par(N);
     if (e == cudaSuccess) e = cudaMemcpyAsync(par.data(), parents, 8 * N, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) {
-        std::vector<long long> off(N + 1, 0), idx(N > 0 ? N : 1);
-        for (long long i = 0; i < N; ++i) if (par[i] >= 0) ++off[par[i] + 1];
+        std::vector<long long> off(N + 1, 0), idx(N > 0 ? N : 1), rl;
+        for (long long i = 0; i < N; ++i) if (par[i] >= 0) ++off[par[i] + 1]; else rl.push_back(i);
         for (long long i = 0; i < N; ++i) off[i + 1] += off[i];
         std::vector<long long> fillp(off.begin(), off.end() - 1);
         for (long long i = 0; i < N; ++i) if (par[i] >= 0) idx[fillp[par[i]]++] = i;
+        n_roots = (int64_t)rl.size();
         e = cudaMemcpyAsync(child_off, off.data(), 8 * (N + 1), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(child_idx, idx.data(), 8 * N, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && !rl.empty()) e = cudaMemcpyAsync(roots, rl.data(), 8 * rl.size(), cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     }
-    cudaFree(order32); cudaFree(act); cudaFree(act2); cudaFree(counters); cudaFree(mask); cudaFree(state);
+    float ms = 0.f;
+    if (e == cudaSuccess) {
+        cudaEventRecord(ev1, st);
+        cudaEventSynchronize(ev1);
+        cudaEventElapsedTime(&ms, ev0, ev1);
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    build_ms = ms;
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "tree build: %s", cudaGetErrorString(e));
     has_tree = true;
     return CT_OK;

@@ -20,6 +20,8 @@ struct BruteParams {
     float var;
     long long* out_idx;
     float* out_dist;
+    // candidate rows [cbeg, cend); cend <= 0 means n (every row)
+    long long cbeg = 0, cend = 0;
 };
 
 size_t brute_smem_bytes(int qt, int m, int d, int k);

@@ -2102,7 +2102,7 @@ long long ct_tree::device_bytes() const {
     const long long rows = n + std::max<long long>(slab_rows, screen ? ((const State*)screen)->slab_cap : 0);
     long long b = (long long)n * m * 4 + n * (long long)d * 4 + n * 8 + 64 * 4;  // vperm, xs (dataset part), norms, p
     b += rows * (long long)m * 4 + rows * (long long)d * 8 + rows * 4;           // vnat, coords_raw + slab xs, slab p
-    if (has_tree) b += n * (8 * 6 + 4 + 4) + (long long)n * (m + d + 2) * 4;
+    if (has_tree) b += n * (8 * 7 + 4 * 6) + (long long)n * (m + d + 2) * 4;
     if (screen) {
         const State* S = (const State*)screen;
         b += S->rows_pad * (long long)m * 4 + S->lvl_rows * (long long)m * 4;   // hi + lo BF16 operands

@@ -33,7 +33,7 @@ int ct_tree::alloc_metric() {
 ct_tree::~ct_tree() {
     release_screen();
     dfree(vperm); dfree(xs); dfree(norms); dfree(p); dfree(inv_ls); dfree(vnat); dfree(coords_raw);
-    dfree(order); dfree(inv); dfree(parents); dfree(levels); dfree(si); dfree(sub_min);
-    dfree(child_off); dfree(child_idx); dfree(roots);
-    dfree(tvnat); dfree(txs); dfree(tnorms); dfree(tp);
+    dfree(order); dfree(inv); dfree(parents); dfree(levels); dfree(si); dfree(si_up); dfree(sub_isp);
+    dfree(sub_min); dfree(child_off); dfree(child_idx); dfree(roots);
+    dfree(tvnat); dfree(txs); dfree(tnorms); dfree(tp); dfree(tisp); dfree(tvn);
 }

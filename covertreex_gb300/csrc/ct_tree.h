@@ -6,6 +6,7 @@
 #include <stdio.h>
 
 #include "../../include/covertree_cuda.h"
+#include "ct_treebound.cuh"
 
 struct ct_tree {
     // shape and metric parameters
@@ -33,7 +34,9 @@ struct ct_tree {
     long long* inv = nullptr;       // dataset -> node
     long long* parents = nullptr;   // node numbering, -1 for roots
     int32_t* levels = nullptr;
-    float* si = nullptr;          // cover radius (max distance to any descendant, upper bound)
+    float* si = nullptr;          // cover radius: max FP32 distance to any descendant
+    float* si_up = nullptr;       // certified upper bound of the ideal-metric cover radius
+    float* sub_isp = nullptr;     // max 1/sqrt(p) over the subtree (node itself included)
     long long* sub_min = nullptr;   // min dataset id in the subtree (node itself included)
     long long* child_off = nullptr; // CSR children: child_off[n+1], child_idx[n]
     long long* child_idx = nullptr;
@@ -43,6 +46,13 @@ struct ct_tree {
     float* txs = nullptr;
     float* tnorms = nullptr;
     float* tp = nullptr;
+    float* tisp = nullptr;        // node order: 1/sqrt(p) and ||v||, both rounded up
+    float* tvn = nullptr;
+    int64_t n_side = 0;           // rows kept out of the tree (tiny p), the last n_side nodes
+    ct::BoundModel bound{};       // error model of the certified prune (ct_treebound.cuh)
+    // build telemetry
+    int64_t build_groups = 0, build_conflict_edges = 0, build_selected = 0;
+    float build_ms = 0.f;
 
     // screened form (BF16 operands, built lazily)
     void* screen = nullptr;

@@ -216,6 +216,16 @@ class CudaResidualIndex:
         return {"parents": parents.cpu().numpy(), "levels": levels.cpu().numpy(), "si": si.cpu().numpy(),
                 "node_to_dataset": order.cpu().numpy(), "subtree_min": smin.cpu().numpy()}
 
+    def build_info(self) -> dict:
+        """Telemetry of the device cover-tree build (``ct_tree_build_info``)."""
+        vals = [ctypes.c_int64() for _ in range(5)]
+        ms = ctypes.c_double()
+        _lib.check(_lib.load().ct_tree_build_info(self._h, *[ctypes.byref(v) for v in vals], ctypes.byref(ms)))
+        keys = ("groups", "conflict_edges", "selected", "side_rows", "roots")
+        out = {k: int(v.value) for k, v in zip(keys, vals)}
+        out["build_ms"] = float(ms.value)
+        return out
+
     def free(self):
         if getattr(self, "_h", None) is not None and self._h.value:
             _lib.load().ct_free(self._h)

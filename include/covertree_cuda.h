@@ -103,7 +103,8 @@ CT_API const char* ct_last_error(void);
  *   lengthscale: HOST pointer to n_lengthscale floats (missing axes reuse entry 0,
  *   |l| < 1e-6 is clamped to 1e-6, src/metric.rs:93-101).
  *   variance: kernel variance (rbf_var).  kernel_type: CT_KERNEL_*.
- *   chunk: batch-insert chunk size (reference default 512).  order: CT_ORDER_*.
+ *   chunk: the reference's batch-insert chunk size, accepted for its signature; the
+ *   device build inserts prefix-doubling groups instead (ct_build.cu).  order: CT_ORDER_*.
  *   seed: MIS seed.  flags: CT_BUILD_*.
  * The inputs are copied; the caller may free them after the call returns.
  * Synchronises `stream` once at the end of the build.
@@ -203,6 +204,13 @@ CT_API int ct_tree_device_bytes(const ct_tree* tree, int64_t* bytes);
  * order; device f32; any may be NULL), e.g. to persist the tree.  No counterpart in
  * the reference, which has no tree persistence. */
 CT_API int ct_tree_inputs(const ct_tree* tree, float* v, float* p, float* coords, void* stream);
+
+/* Telemetry of the cover-tree build (host outputs; any may be NULL), the counterpart of
+ * the reference's BatchInsertTelemetry (src/algo/batch/mod.rs): prefix-doubling groups
+ * inserted, conflict-graph edges stored, points selected by the MIS, rows kept out of
+ * the tree (tiny residual variance, scored by every query), roots, build milliseconds. */
+CT_API int ct_tree_build_info(const ct_tree* tree, int64_t* groups, int64_t* conflict_edges, int64_t* selected,
+                              int64_t* side_rows, int64_t* roots, double* build_ms);
 
 /* n, m, d of a tree (host outputs; any may be NULL). */
 CT_API int ct_tree_shape(const ct_tree* tree, int64_t* n, int32_t* m, int32_t* d);

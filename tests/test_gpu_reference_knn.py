@@ -47,12 +47,7 @@ def test_forms_match_reference_knn(cuda_available, ci, form):
     assert np.array_equal(gi >= 0, c["idx"] >= 0)
     good = c["p"] >= 1e-3
     same = np.array([set(a[a >= 0]) == set(b[b >= 0]) for a, b in zip(gi, c["idx"])])
-    if form == "tree":
-        # the tree form's cover-radius prune is checked row by row where its bounds are
-        # certified (see test_gpu_tree.py); here every well-conditioned row must agree
-        assert same[good].mean() >= 0.99
-    else:
-        assert same[good].all(), np.nonzero(good & ~same)[0][:10]
+    assert same[good].all(), np.nonzero(good & ~same)[0][:10]
     v = (c["idx"] >= 0) & good[:, None] & same[:, None]
     assert np.abs(np.sort(np.where(v, gd, 0), 1) - np.sort(np.where(v, c["dist"], 0), 1)).max() < 5e-3
     if c["pred"]:

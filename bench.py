@@ -52,6 +52,9 @@ def parse_args():
     ap.add_argument("--no-headline", action="store_true",
                     help="skip the precision-form workload (profiling the batching form alone)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-form measurement")
+    ap.add_argument("--no-euclidean", action="store_true", help="skip the Euclidean k=10 measurement")
+    ap.add_argument("--no-tree", action="store_true", help="skip the cover-tree form measurement")
+    ap.add_argument("--tree-queries", type=int, default=4096, help="sampled queries of the tree-form measurement")
     ap.add_argument("--serving-rates", default="100,500,1000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--serving-seconds", type=float, default=2.0, help="arrival window per serving rate")
     return ap.parse_args()
@@ -264,6 +267,83 @@ def fp64_check(wl, dev, rows, got_idx, got_dist, near_tie=1e-6, block=256):
                 stats["mismatches_beyond_near_tie"] += 1
         del d2, K, D
     return stats
+
+
+# ------------------------------------------------------------------ Euclidean and tree forms
+def bench_euclidean(dev, steps: int = 3, warmup: int = 3, cpu: bool = True):
+    """README-shape Euclidean run: N=32768 N(0,1) coordinates in D=3 (seed 1), k=10,
+    queries = the coordinates, exact GPU kNN (ct_knn_euclidean); beside it the
+    restated reference Euclidean cover tree (oracle) on a query sample, host cores."""
+    import torch
+
+    from covertreex_gb300 import synthetic
+    from covertreex_gb300.euclidean import EuclideanTree
+
+    X = synthetic.gaussian_coords(32768, 3, 1)
+    tree = EuclideanTree(X, device=dev)
+    q = torch.as_tensor(X, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(warmup):
+        tree.knn_device(q, 10)
+    torch.cuda.synchronize(dev)
+    ms = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        tree.knn_device(q, 10)
+        b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    step_ms = float(np.mean(ms))
+    out = {"workload": "Euclidean kNN, N=32768, D=3, N(0,1) seed 1, k=10, queries = coordinates (exact)",
+           "queries_per_s": 32768 / (step_ms / 1e3), "ms_per_step": step_ms, "steps": steps,
+           "gpu_launches_per_step": 1}
+    if cpu:
+        from oracle import oracle as O
+
+        threads = os.cpu_count() or 1
+        ot = O.OracleEuclideanTree(X)
+        sample = X[np.random.default_rng(4).choice(32768, 4096, replace=False)]
+        t0 = time.perf_counter()
+        ot.knn(sample, 10)
+        dt = time.perf_counter() - t0
+        out["cpu_reference"] = {"value": sample.shape[0] / dt, "unit": "queries/s", "cores": threads,
+                                "kind": "port", "sample": "4096 random coordinates as queries (restated "
+                                "rust Euclidean cover tree, best-first, approximate as the reference)"}
+    return out
+
+
+def bench_tree(wl, dev, nsample: int):
+    """Cover-tree form on the same workload: device build seconds (prefix-doubling groups,
+    conflict graph, MIS, certified radii) and the exact traversal on `nsample` sampled
+    queries, with the distance evaluations per query (the reference's E_q) beside the
+    dense form's."""
+    import torch
+
+    from covertreex_gb300 import _lib
+    from covertreex_gb300.device import CudaResidualIndex
+
+    L = _lib.load()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    idx = CudaResidualIndex(wl.v, wl.p, wl.coords, variance=wl.variance, lengthscale=[wl.lengthscale] * wl.d,
+                            kernel_type=wl.kernel_type, build_tree=True, device=dev)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    info = idx.build_info()
+    q = np.sort(np.random.default_rng(4).choice(wl.n, min(nsample, wl.n), replace=False))
+    L.ct_set_timing(1)
+    ti, td = idx.knn(q, wl.k, predecessor=wl.predecessor, form="tree")
+    st = dict(idx.last_stats)
+    di, dd = idx.knn(q, wl.k, predecessor=wl.predecessor, form="dense")
+    same = bool(np.array_equal(ti, di) and np.array_equal(td.view(np.uint32), dd.view(np.uint32)))
+    dense_pairs = float(np.sum(q)) if wl.predecessor else float(q.size) * wl.n
+    idx.free()
+    return {"workload": wl.describe() + f" (tree form, {q.size} sampled queries)",
+            "build_s": info["build_ms"] / 1e3, "build_wall_s": wall, "build": info,
+            "queries_per_s": q.size / (st["device_ms"] / 1e3) if st["device_ms"] else None,
+            "ms": st["device_ms"], "distance_evals_per_query": st["distance_evals"] / q.size,
+            "dense_pairs_per_query": dense_pairs / q.size, "identical_to_dense": same}
 
 
 # ------------------------------------------------------------------ batching form
@@ -576,6 +656,8 @@ def main():
 
     batching = None
     serving = None
+    euclid = None
+    tree = None
     if rank == 0 and world == 1 and not args.no_batching:
         try:
             batching = bench_batching(dev, count=args.batch_trees)
@@ -588,6 +670,17 @@ def main():
         except Exception as exc:
             serving = {"unavailable": repr(exc)}
 
+    # ---- Euclidean and tree forms (after serving: the Euclidean CPU reference starts an OpenMP pool)
+    if rank == 0 and world == 1 and not args.no_euclidean:
+        try:
+            euclid = bench_euclidean(dev, cpu=not args.no_cpu_baseline)
+        except Exception as exc:
+            euclid = {"unavailable": repr(exc)}
+    if rank == 0 and world == 1 and not args.no_tree:
+        try:
+            tree = bench_tree(wl, dev, args.tree_queries)
+        except Exception as exc:
+            tree = {"unavailable": repr(exc)}
     # ---- CPU baseline (rank 0, N=1 only): restated rust-hilbert on host cores, last,
     # so that its OpenMP thread pool does not share the host with the serving loop
     cpu = None
@@ -634,6 +727,8 @@ def main():
             "wall_s_timed": t_wall,
             "batching": batching,
             "serving": serving,
+            "euclidean": euclid,
+            "tree": tree,
         }
         print(json.dumps(line))
     if dist is not None:

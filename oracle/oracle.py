@@ -276,7 +276,10 @@ class OracleResidualTree:
         evals = L.ct_oracle_knn_residual(self._h, _p(q, _i64p), q.size, int(k), int(predecessor),
                                          _p(self.subtree_min, _i64p), int(par), _p(oi, _i64p), _p(od, _f32p),
                                          int(threads))
+        # the reference's `distance_evals` (src/algo.rs:1087-1092) counts the batch-path
+        # child evaluations only; every query also scores every root (algo.rs:688-734)
         self.last_evals = int(evals)
+        self.last_root_evals = int(q.size) * int(np.count_nonzero(self.parents == -1))
         return oi, od
 
     def __del__(self):

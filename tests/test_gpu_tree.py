@@ -71,8 +71,10 @@ def test_traversal_equals_dense_on_every_row(cuda_available, predecessor):
     # the reference's parity mode on the same inputs (oracle restatement), for scale
     ref = O.OracleResidualTree(case["V"], case["p"], case["X"], 1.0, case["ls"], kernel_type=1, parity=True)
     ref.knn(q[::16], 50, predecessor=predecessor, parity=True)
-    print(f"N=8192 predecessor={predecessor}: device tree {evals / q.size:.0f} distance evaluations per query, "
-          f"reference parity mode {ref.last_evals / q[::16].size:.0f}; build {idx.build_info()}")
+    nq_ref = q[::16].size
+    print(f"N=8192 predecessor={predecessor}: device tree {evals / q.size:.0f} distance evaluations per query; "
+          f"reference parity mode {ref.last_evals / nq_ref:.0f} child evaluations + "
+          f"{ref.last_root_evals / nq_ref:.0f} root distances per query; build {idx.build_info()}")
 
 
 def test_traversal_d8_mixture_equals_dense(cuda_available):

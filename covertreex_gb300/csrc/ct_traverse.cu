@@ -9,8 +9,8 @@
 // then the children of each expanded node) are filtered 32 at a time with a ballot
 // (predecessor mode: a subtree whose minimum dataset id is not below the query's is
 // skipped without a distance, src/algo.rs:900-916), and the surviving candidates are
-// scored 8 at a time: their V rows are staged in shared memory with 16-byte cp.async
-// copies, then each half-warp scores 4 rows with the reference's batch-path f32
+// scored 4 at a time: their V rows are staged in shared memory with 16-byte cp.async
+// copies, then each half-warp scores 2 rows with the reference's batch-path f32
 // distance (lane l sums elements 16c + l, bit-identical to the dense form) against
 // the query row held in registers.
 //
@@ -33,10 +33,13 @@
 namespace ct {
 namespace trav {
 
-constexpr int kWarps = 4;
-constexpr int kStack = 33 * 32 + 1;  // 33 frames per level of at most 32 levels, + the roots
+constexpr int kWarps = 8;
+constexpr int kChunk = 8;                    // list entries a frame hands out per step
+// per tree level the stack holds at most one chunk's children; 40 levels (levels fall strictly
+// from 0 to -30, and only duplicate points share the floor level)
+constexpr int kStack = kChunk * 40 + 1;
 constexpr int kTopK = 64;
-constexpr int kRows = 8;  // candidate rows staged per batch (4 per half-warp)
+constexpr int kRows = 4;  // candidate rows staged per batch (2 per half-warp)
 
 struct Params {
     const float* v;      // node-order natural V
@@ -130,8 +133,9 @@ __global__ void __launch_bounds__(32 * kWarps) traverse_kernel(Params P) {
             const bool may_prune = isq <= kNoPruneIsp;
             bool overflowed = false;
             // Depth-first over frames (node, cursor, bound): node -1 is the list of roots.
-            // A frame hands out its candidates 32 at a time; expandable candidates become
-            // frames on top of it, so the stack holds at most 33 frames per tree level.
+            // A frame hands out its candidates kChunk at a time; expandable candidates
+            // become frames on top of it, so the stack holds at most kChunk frames per tree
+            // level; a deeper tree is reported as an overflow error, never read past.
             int sp = 0;
             if (lane == 0) { stn[0] = -1; stc[0] = 0; stl[0] = 0.f; }
             sp = 1;
@@ -151,9 +155,9 @@ __global__ void __launch_bounds__(32 * kWarps) traverse_kernel(Params P) {
                     --sp;
                     continue;
                 }
-                if (lane == 0) stc[top] = cur + 32;
+                if (lane == 0) stc[top] = cur + kChunk;
                 const long long gi = base + lane;
-                int c = gi < e0 ? (int)ids[gi] : -1;
+                int c = (lane < kChunk && gi < e0) ? (int)ids[gi] : -1;
                 if (c >= 0 && P.predecessor && P.sub_min[c] >= qd) c = -1;
                 const unsigned ok = __ballot_sync(0xffffffffu, c >= 0);
                 if (c >= 0) cand[__popc(ok & ((1u << lane) - 1u))] = c;

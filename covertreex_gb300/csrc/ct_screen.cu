@@ -63,6 +63,8 @@ constexpr int kThreads = 96 + kEpiThreads;  // producer, MMA issuer, staging, ep
 constexpr int kMaxD = 8;
 constexpr int kMaxK = 64;                   // heap capacity per epilogue thread
 constexpr int REC = 12;                     // floats per staged candidate record
+constexpr int GREC = 20;                    // floats per group record (8 consecutive candidates)
+constexpr int RT = TC * REC + (TC / 8) * GREC;  // floats of one candidate tile's records
 constexpr int kSurvCap = 1024;  // survivors per query slot (two column halves), at most RBUF
 constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
 static_assert(kSurvCap <= RBUF, "a slot's survivors must fit the rescoring buffer");
@@ -105,7 +107,7 @@ struct MMAParams {
     float* out_f;        // debug output
     int* surv; int* surv_cnt;
     int half_cap;        // survivor segment per (slot, column half)
-    const float* rec[2]; // candidate records in tile order (levels, dataset), TC * REC floats per tile
+    const float* rec[2]; // candidate records in tile order (levels, dataset), RT floats per tile
     const unsigned* xmax_max;  // bits of max |x_c| over the dataset rows
     int* status;
     unsigned* qtau;      // per query (slot / parts): the smallest part threshold, float bits
@@ -119,7 +121,7 @@ __host__ __device__ inline SmemLayout smem_layout(int k, int nstages) {
     SmemLayout L;
     size_t off = 0;
     L.stages = off; off += (size_t)nstages * STAGE_BYTES;
-    L.rec = off; off += (size_t)2 * TC * REC * sizeof(float);
+    L.rec = off; off += (size_t)2 * RT * sizeof(float);
     L.heap = off; off += (size_t)kEpiThreads * (k > 0 ? k : 1) * sizeof(float);
     L.rowtau = off; off += (size_t)TQ * sizeof(unsigned long long);
     L.bars = off; off += (size_t)(2 * STAGES + 4 + 4 + 1) * 8;
@@ -273,9 +275,9 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 const int acc = lt & 1;
                 const unsigned aph = (unsigned)((lt >> 1) & 1);
                 if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) break;
-                sm::mbar_arrive_expect_tx(&recf[acc], (unsigned)(TC * REC * sizeof(float)));
-                sm::bulk_g2s(recs + (size_t)acc * TC * REC, P.rec[jb.which & 1] + (size_t)jb.ctile * TC * REC,
-                             (unsigned)(TC * REC * sizeof(float)), &recf[acc]);
+                sm::mbar_arrive_expect_tx(&recf[acc], (unsigned)(RT * sizeof(float)));
+                sm::bulk_g2s(recs + (size_t)acc * RT, P.rec[jb.which & 1] + (size_t)jb.ctile * RT,
+                             (unsigned)(RT * sizeof(float)), &recf[acc]);
             }
         }
     } else {
@@ -303,6 +305,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         // Kernel-value error bound of the query, linear in d2 (see phase 1): for RBF the
         // relative factor fk = alk d2 + bek, for Matern the d2 error ed2 = ale d2 + bee.
         float alk = 0.f, bek = 0.f, ale = 0.f, bee = 0.f;
+        // Largest kernel-value error term ek of any pair of the query (the maxima over d2
+        // of the expressions below: x e^-x/2 <= 2/e for RBF; for Matern 5/2 with
+        // a = sqrt(5 d2): a (1 + a + a^2/3) e^-a <= 1.176, a^2 (1 + a) e^-a <= 1.814,
+        // (1 + a) e^-a <= 1), used by the group test.
+        float ekmax = 0.f;
         // keep the pair iff (R + e) * isc >= thr_keep; it may enter the heap iff
         // (R - e) * isc > thr_heap, i.e. its d^2 upper bound is below tau2 (both derived
         // from tau2: a pair at or above the row's threshold cannot lower it, since the
@@ -338,6 +345,8 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     bee = 0.5f * A * 1.00001f;
                     alk = (6e-8f + 0.5f * ced2 + 0.25f * A * dd) * 1.00001f;
                     bek = (1e-6f + 0.25f * A) * 1.00001f;
+                    ekmax = KT == 0 ? P.var * (0.7358f * alk + bek) * 1.01f
+                                    : P.var * (1.283e-6f + 0.8334f * (0.3628f * ale + bee) + 1.82e-7f) * 1.01f;
                 }
                 thr_keep = 0.f;   // tau2 = 1: keep everything
                 thr_heap = 0.f;   // and heap every pair whose |rho| bound is positive
@@ -345,7 +354,8 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) break;
             if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) break;
             sm::tc_fence_after();
-            const float* rb = recs + (size_t)acc * TC * REC;
+            const float* rb = recs + (size_t)acc * RT;
+            const float* gtab = rb + TC * REC;  // group records of the tile
             const bool keep_job = !(jb.which & 2);
             const bool feed_heap = !(jb.which & 4);
             const bool fast_ids = (jb.which & 8) != 0;
@@ -380,6 +390,45 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     continue;
                 }
                 if (qid < 0) continue;
+                // Group test: one certified bound for the group's 8 pairs.  The group record
+                // holds the box of the 8 candidates' scaled coordinates, their largest
+                // err_coef |v_c| and 1/sqrt(p_c).  The box's nearest and farthest points give
+                // bounds Kmax >= kv >= Kmin of the kernel value phase 1 would compute (its
+                // f32 coordinate distance, __expf and Matern polynomial, within the relative
+                // margins), so |kv - s| <= max(Kmax - s, s - Kmin) and phase 1's survivor
+                // bound is at most hi.  hi < thr_keep (<= thr_heap) means no pair of the group
+                // is kept or heaped: the group is done without phase 1.  Where the kernel
+                // value is negligible (candidates far from the query in coordinates) this
+                // skips the per-pair work; padding groups (NaN 1/sqrt(p)) always skip.
+                {
+                    const float* gr = gtab + (size_t)(col0 >> 3) * GREC;
+                    float dmin = 0.f, dmax = 0.f;
+#pragma unroll
+                    for (int c = 0; c < DP; ++c) {
+                        const float a = gr[c] + nxq[c];      // lo_c - x_q,c
+                        const float b = gr[8 + c] + nxq[c];  // hi_c - x_q,c
+                        const float t = fmaxf(fmaxf(a, -b), 0.f);
+                        dmin = fmaf(t, t, dmin);
+                        const float u = fmaxf(fabsf(a), fabsf(b));
+                        dmax = fmaf(u, u, dmax);
+                    }
+                    dmin *= (1.f - 1e-5f);
+                    dmax *= (1.f + 1e-5f);
+                    float kmax, kmin;
+                    if (KT == 0) {
+                        kmax = P.var * __expf(-0.5f * dmin) * (1.f + 1e-5f);
+                        kmin = P.var * __expf(-0.5f * dmax) * (1.f - 1e-5f);
+                    } else {
+                        const float a0 = 2.2360679775f * sqrtf(dmin), a1 = 2.2360679775f * sqrtf(dmax);
+                        kmax = P.var * (1.f + a0 + a0 * a0 * 0.33333334f) * __expf(-a0) * (1.f + 2e-5f);
+                        kmin = P.var * (1.f + a1 + a1 * a1 * 0.33333334f) * __expf(-a1) * (1.f - 2e-5f);
+                    }
+                    float rmax = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) rmax = fmaxf(rmax, fmaxf(kmax - v[i], v[i] - kmin));
+                    const float ghi = (rmax * (1.f + 3e-7f) + vnq * gr[16] + ekmax + 1e-30f) * gr[17] * (1.f + 1e-6f);
+                    if (!(ghi >= thr_keep)) continue;
+                }
                 // Phase 1, no stores: certified bounds of the group's 8 pairs, as
                 //   blo = (R - e) * isc (heap test)  and  bhi = (R + e) * isc (survivor test),
                 // +inf for the query itself, -inf for predecessor-violating pairs and NaN for
@@ -516,7 +565,7 @@ __global__ void build_records_kernel(const int* __restrict__ ids, long long rows
     if (r >= rows) return;
     const long long tile = r / TC;
     const int e = (int)(r - tile * TC);
-    float* o = rec + tile * (TC * REC) + (e >> 1) * (2 * REC) + (e & 1);
+    float* o = rec + tile * RT + (e >> 1) * (2 * REC) + (e & 1);
     const int cid = ids[r];
     if (cid >= 0) {
 #pragma unroll
@@ -531,6 +580,44 @@ __global__ void build_records_kernel(const int* __restrict__ ids, long long rows
         o[18] = __int_as_float(0x7fc00000);  // NaN 1/sqrt(p): every bound test of the row fails
         o[22] = __int_as_float(-1);
     }
+}
+
+// Group records of the sweep's group test, one per 8 consecutive candidates of a tile
+// (after the tile's candidate records): the box of their scaled coordinates (lo in
+// floats 0-7, hi in 8-15; 0 past d), the largest err_coef |v| (16) and 1/sqrt(p) (17).
+// A group without a valid row gets an empty box (+inf, -inf) and NaN 1/sqrt(p).
+__global__ void build_group_records_kernel(const int* __restrict__ ids, long long rows, const float* __restrict__ xs,
+                                           int d, const float* __restrict__ vn, const float* __restrict__ isp,
+                                           float err_coef, float* __restrict__ rec) {
+    const long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (gi >= rows / 8) return;
+    const long long tile = gi / (TC / 8);
+    const int g = (int)(gi - tile * (TC / 8));
+    float lo[kMaxD], hi[kMaxD];
+#pragma unroll
+    for (int c = 0; c < kMaxD; ++c) { lo[c] = __int_as_float(0x7f800000); hi[c] = -__int_as_float(0x7f800000); }
+    float emax = 0.f, imax = __int_as_float(0x7fc00000);
+    bool any = false;
+    for (int e = 0; e < 8; ++e) {
+        const int cid = ids[tile * TC + 8 * g + e];
+        if (cid < 0) continue;
+#pragma unroll
+        for (int c = 0; c < kMaxD; ++c) {
+            const float x = c < d ? xs[(size_t)cid * d + c] : 0.f;
+            lo[c] = fminf(lo[c], x);
+            hi[c] = fmaxf(hi[c], x);
+        }
+        emax = fmaxf(emax, err_coef * vn[cid]);
+        imax = any ? fmaxf(imax, isp[cid]) : isp[cid];
+        any = true;
+    }
+    float* o = rec + tile * RT + TC * REC + (size_t)g * GREC;
+#pragma unroll
+    for (int c = 0; c < kMaxD; ++c) { o[c] = lo[c]; o[8 + c] = hi[c]; }
+    o[16] = emax;
+    o[17] = imax;
+    o[18] = 0.f;
+    o[19] = 0.f;
 }
 
 // hi/lo split of V rows into the blocked layout.  rowmap[r] = dataset row of
@@ -1574,8 +1661,8 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
     A((void**)&S->xmax, sizeof(float) * rows_q);
     A((void**)&S->isp_max, sizeof(unsigned));
     A((void**)&S->xmax_max, sizeof(unsigned));
-    A((void**)&S->rec_ds, sizeof(float) * REC * S->rows_pad);
-    A((void**)&S->rec_lvl, sizeof(float) * REC * S->lvl_rows);
+    A((void**)&S->rec_ds, sizeof(float) * RT * (S->rows_pad / TC));
+    A((void**)&S->rec_lvl, sizeof(float) * RT * (S->lvl_rows / TC));
     A((void**)&S->inv_ls64, sizeof(double) * 64);
     A((void**)&S->inv_ls_df, sizeof(float) * 128);
     A((void**)&S->status, sizeof(int));
@@ -1624,6 +1711,10 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
                                                                     S->isp, S->xmax, ec, S->rec_ds);
         build_records_kernel<<<grid_for(S->lvl_rows), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs, T->d, S->vn,
                                                                     S->isp, S->xmax, ec, S->rec_lvl);
+        build_group_records_kernel<<<grid_for(S->rows_pad / 8), 256, 0, st>>>(S->b_id_ds, S->rows_pad, T->xs, T->d,
+                                                                             S->vn, S->isp, ec, S->rec_ds);
+        build_group_records_kernel<<<grid_for(S->lvl_rows / 8), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs, T->d,
+                                                                              S->vn, S->isp, ec, S->rec_lvl);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -2107,6 +2198,7 @@ long long ct_tree::device_bytes() const {
         const State* S = (const State*)screen;
         b += S->rows_pad * (long long)m * 4 + S->lvl_rows * (long long)m * 4;   // hi + lo BF16 operands
         b += S->rows_pad * 4 + S->lvl_rows * 12 + n * 12 + rows * 20 + 1024;
+        b += (S->rows_pad + S->lvl_rows) / TC * (long long)RT * 4;                  // sweep records
     }
     return b;
 }

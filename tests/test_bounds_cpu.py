@@ -136,7 +136,7 @@ def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls):
     assert np.median(widths) < 1e-3, np.median(widths)
 
 
-def epilogue_rho_bounds(q, c, data, v_mma, exp_pick):
+def epilogue_rho_bounds(q, c, data, v_mma, exp_pick, raw=False):
     """Lower / upper bounds of |rho| the sweep epilogue derives for one pair from a tensor-core
     dot v_mma: the heap uses max(blo, 0) isq (1 - 1e-6), the survivor test bhi isq / (1 - 2e-6)."""
     Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
@@ -171,6 +171,8 @@ def epilogue_rho_bounds(q, c, data, v_mma, exp_pick):
     e = F(fma32(vnq, err_c, ek) + fma32(R, F(1.2e-7), F(1e-30)))
     blo = F(F(R + F(-e)) * isc)
     bhi = F(F(R + e) * isc)
+    if raw:
+        return blo, bhi
     rho_lo = float(F(F(max(blo, F(0.0)) * isq) * F(1.0 - 1e-6)))
     rho_hi = float(bhi) * float(isq) / (1.0 - 2e-6)
     return rho_lo, rho_hi
@@ -204,3 +206,102 @@ def test_epilogue_bounds_contain_fp64(n, d, m, kt, ls):
             for pick in (0, 1, 2):
                 lo, hi = epilogue_rho_bounds(q, c, data, v_mma, pick)
                 assert lo <= rho_true <= hi, (q, c, float(v_mma), pick, lo, rho_true, hi)
+
+
+def _query_consts(q, data):
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    dd = F(d)
+    ced2 = F(F(dd + F(2.0)) * F(5.97e-8))
+    A = F(F(2.4e-7) * F(xmax[q] + xmax_max))
+    ale = F(F(ced2 + F(F(F(0.5) * A) * dd)) * F(1.00001))
+    bee = F(F(F(0.5) * A) * F(1.00001))
+    alk = F(F(F(F(6e-8) + F(F(0.5) * ced2)) + F(F(F(0.25) * A) * dd)) * F(1.00001))
+    bek = F(F(F(1e-6) + F(F(0.25) * A)) * F(1.00001))
+    if kt == 0:
+        ekmax = F(F(F(var) * F(F(F(0.7358) * alk) + bek)) * F(1.01))
+    else:
+        ekmax = F(F(F(var) * F(F(F(1.283e-6) + F(F(0.8334) * F(F(F(0.3628) * ale) + bee))) + F(1.82e-7))) * F(1.01))
+    return ekmax
+
+
+def group_hi(q, cands, data, v_mmas, kpick):
+    """The sweep epilogue's group test (screen_sweep_kernel), float32 operation by operation:
+    a bound on phase 1's survivor bound bhi of every pair of the group.  kpick selects
+    __expf at either end of its error band for Kmax (low end) and Kmin (high end)."""
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    u2 = 1.0 / 65536.0
+    err_coef = F(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22)
+    lo = xs[cands].min(axis=0)
+    hi = xs[cands].max(axis=0)
+    err_max = max(F(err_coef * vn[c]) for c in cands)
+    isc_max = max(isp[c] for c in cands)
+    dmin = F(0.0)
+    dmax = F(0.0)
+    for a_ in range(d):
+        a = F(lo[a_] + F(-xs[q, a_]))
+        b = F(hi[a_] + F(-xs[q, a_]))
+        t = max(max(a, F(-b)), F(0.0))
+        dmin = fma32(t, t, dmin)
+        u = max(abs(a), abs(b))
+        dmax = fma32(u, u, dmax)
+    dmin = F(dmin * F(1.0 - 1e-5))
+    dmax = F(dmax * F(1.0 + 1e-5))
+    lo_e, hi_e = (1, 2) if kpick else (0, 0)
+    if kt == 0:
+        kmax = F(F(F(var) * expf_band(F(F(-0.5) * dmin))[lo_e]) * F(1.0 + 1e-5))
+        kmin = F(F(F(var) * expf_band(F(F(-0.5) * dmax))[hi_e]) * F(1.0 - 1e-5))
+    else:
+        a0 = F(F(2.2360679775) * F(np.sqrt(dmin)))
+        a1 = F(F(2.2360679775) * F(np.sqrt(dmax)))
+        kmax = F(F(F(F(var) * F(F(F(1.0) + a0) + F(F(a0 * a0) * F(0.33333334)))) * expf_band(F(-a0))[lo_e]) * F(1.0 + 2e-5))
+        kmin = F(F(F(F(var) * F(F(F(1.0) + a1) + F(F(a1 * a1) * F(0.33333334)))) * expf_band(F(-a1))[hi_e]) * F(1.0 - 2e-5))
+    rmax = F(0.0)
+    for v in v_mmas:
+        rmax = max(rmax, max(F(kmax - v), F(v - kmin)))
+    ekmax = _query_consts(q, data)
+    inner = F(F(F(rmax * F(1.0 + 3e-7)) + F(vn[q] * err_max)) + F(ekmax + F(1e-30)))
+    return F(F(inner * isc_max) * F(1.0 + 1e-6))
+
+
+@pytest.mark.parametrize("n,d,m,kt,ls", [
+    (1500, 8, 64, 0, 2.0),   # RBF, precision-workload-like
+    (1500, 3, 64, 1, 1.0),   # Matern 5/2
+    (1200, 3, 128, 0, 0.7),  # RBF, short lengthscale
+    (1200, 5, 96, 1, 2.0),   # Matern, D = 5
+])
+def test_group_test_bounds_every_pair(n, d, m, kt, ls):
+    """The sweep's group test never rejects a group holding a pair that phase 1 would keep
+    or heap: its bound is >= phase 1's survivor bound bhi of every pair, for tensor-core dots
+    anywhere in the certified band, __expf at either end of its band, for groups of 8 points
+    close together (coordinate-sorted, tight boxes), random groups, groups holding the query
+    itself and groups with tiny-p rows."""
+    X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m + 5)
+    xs, vn = data[1], data[2]
+    u2 = 1.0 / 65536.0
+    c_split = 3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22
+    r = np.random.default_rng(23)
+    order = np.lexsort(tuple(xs[:, a] for a in range(d)))  # coordinate-sorted: neighbours in groups of 8
+    groups = [order[8 * g:8 * g + 8] for g in r.choice(n // 8, 12, replace=False)]
+    groups += [r.choice(n, 8, replace=False) for _ in range(8)]
+    groups += [np.concatenate([idx[:2], r.choice(n, 6, replace=False)])]
+    queries = list(r.choice(n, 6, replace=False)) + [int(idx[0])]
+    for q in queries:
+        gq = groups + [np.concatenate([[q], r.choice(n, 7, replace=False)])]
+        for cands in gq:
+            cands = [int(c) for c in cands]
+            for shift in (-1.0, 0.0, 1.0):
+                v_mmas = []
+                for c in cands:
+                    exact = float(np.dot(V[q].astype(np.float64), V[c].astype(np.float64)))
+                    v_mmas.append(F(exact + shift * c_split * float(vn[q]) * float(vn[c])))
+                for kpick in (0, 1):
+                    g = group_hi(q, cands, data, v_mmas, kpick)
+                    for c, v in zip(cands, v_mmas):
+                        if c == q:
+                            continue  # the query itself: phase 1 marks it +inf (never rejected, see below)
+                        for pick in (0, 1, 2):
+                            _, bhi = epilogue_rho_bounds(q, c, data, v, pick, raw=True)
+                            assert g >= bhi, (q, cands, c, float(g), float(bhi))
+                    if q in cands:  # the group holding the query can never be rejected
+                        isq = data[3][q]
+                        assert float(g) >= (1.0 - 2e-6) / float(isq)

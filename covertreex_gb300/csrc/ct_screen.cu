@@ -63,8 +63,12 @@ constexpr int kThreads = 96 + kEpiThreads;  // producer, MMA issuer, staging, ep
 constexpr int kMaxD = 8;
 constexpr int kMaxK = 64;                   // heap capacity per epilogue thread
 constexpr int REC = 12;                     // floats per staged candidate record
-constexpr int GREC = 20;                    // floats per group record (8 consecutive candidates)
-constexpr int RT = TC * REC + (TC / 8) * GREC;  // floats of one candidate tile's records
+// After a tile's candidate records: two half-tile boxes (lo[8], hi[8] of the scaled
+// coordinates of candidates 0-127 and 128-255), then per group of 8 consecutive
+// candidates its largest err_coef |v| and 1/sqrt(p).
+constexpr int HBOX = 16;                    // floats per half-tile box
+constexpr int GREC = 2;                     // floats per group of 8 candidates
+constexpr int RT = TC * REC + 2 * HBOX + (TC / 8) * GREC;  // floats of one candidate tile's records
 constexpr int kSurvCap = 1024;  // survivors per query slot (two column halves), at most RBUF
 constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
 static_assert(kSurvCap <= RBUF, "a slot's survivors must fit the rescoring buffer");
@@ -95,7 +99,12 @@ struct MMAParams {
     const int* b_id[2];  // B row -> dataset id (or -1)
     int m;
     const Job* jobs;
-    const int* cta_job_begin;  // per CTA: [begin, end) into jobs
+    const int* cta_job_begin;  // static schedule: per CTA [begin, end) into jobs (unit_jobs == nullptr)
+    // dynamic schedule: units (query tile, part) as (first job, job count), largest first;
+    // a CTA claims the next unit from unit_counter whenever it needs one
+    const int2* unit_jobs;
+    int nunits;
+    int* unit_counter;
     const int* a_slot;   // A row -> query slot (or -1)
     const int* slot_id;  // query slot -> dataset id
     const float* xs; int d;
@@ -114,8 +123,9 @@ struct MMAParams {
     int parts;           // candidate parts per query (slots s*parts .. s*parts+parts-1)
 };
 
+constexpr int kRing = 4;  // claimed units in flight per CTA (dynamic schedule)
 struct SmemLayout {
-    size_t stages, rec, heap, rowtau, bars, tmem_slot, total;
+    size_t stages, rec, heap, rowtau, bars, tmem_slot, ring, total;
 };
 __host__ __device__ inline SmemLayout smem_layout(int k, int nstages) {
     SmemLayout L;
@@ -124,8 +134,9 @@ __host__ __device__ inline SmemLayout smem_layout(int k, int nstages) {
     L.rec = off; off += (size_t)2 * RT * sizeof(float);
     L.heap = off; off += (size_t)kEpiThreads * (k > 0 ? k : 1) * sizeof(float);
     L.rowtau = off; off += (size_t)TQ * sizeof(unsigned long long);
-    L.bars = off; off += (size_t)(2 * STAGES + 4 + 4 + 1) * 8;
+    L.bars = off; off += (size_t)(2 * STAGES + 4 + 4 + 1 + 2 * kRing) * 8;
     L.tmem_slot = off; off += 16;
+    L.ring = off; off += 16;
     L.total = off + 1024;  // alignment slack
     return L;
 }
@@ -177,12 +188,16 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
     uint64_t* recf = acce + 2;
     uint64_t* rece = recf + 2;
     uint64_t* done = rece + 2;
+    uint64_t* rfull = done + 1;        // unit ring: slot written by the producer
+    uint64_t* rempty = rfull + kRing;  // slot released by every consumer
     uint32_t* tmem_slot = (uint32_t*)(smem + L.tmem_slot);
+    int* ring = (int*)(smem + L.ring);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nchunks = P.m / KC;
     const uint32_t idesc = sm::idesc_bf16_f32(TQ, TC);
-    const int jb0 = P.cta_job_begin[blockIdx.x], jb1 = P.cta_job_begin[blockIdx.x + 1];
+    const int jb0 = P.unit_jobs ? 0 : P.cta_job_begin[blockIdx.x];
+    const int jb1 = P.unit_jobs ? 0 : P.cta_job_begin[blockIdx.x + 1];
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) { sm::mbar_init(&full[s], 1); sm::mbar_init(&empty[s], 1); }
@@ -191,6 +206,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             sm::mbar_init(&recf[a], 1); sm::mbar_init(&rece[a], kEpiWarps);
         }
         sm::mbar_init(done, 1);
+        for (int r = 0; r < kRing; ++r) {
+            sm::mbar_init(&rfull[r], 1);
+            sm::mbar_init(&rempty[r], MODE == MODE_SWEEP ? 2 + kEpiWarps : 1 + kEpiWarps);
+        }
         sm::fence_barrier_init();
     }
     for (int r = threadIdx.x; r < TQ; r += blockDim.x) rowtau[r] = 0ULL;
@@ -203,11 +222,47 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
     sm::tc_fence_after();
     const uint32_t tmem_base = *tmem_slot;
 
+    // The job range of the CTA's ui-th unit.  Static schedule: one range, [jb0, jb1).
+    // Dynamic schedule: the producer claims units into a ring of kRing slots; every other
+    // role takes them from the ring in the same order and releases the slot when done.
+    // A claimed index past the last unit ends every role.
+    auto take_unit = [&](int ui, int& j0, int& j1) -> bool {
+        if (!P.unit_jobs) {
+            j0 = jb0; j1 = jb1;
+            return ui == 0;
+        }
+        const int sl = ui % kRing;
+        if (!sm::mbar_wait(&rfull[sl], (unsigned)((ui / kRing) & 1), P.status, 19)) return false;
+        const int u = *(volatile int*)&ring[sl];
+        if (u < 0) return false;
+        const int2 r = P.unit_jobs[u];
+        j0 = r.x; j1 = r.x + r.y;
+        return true;
+    };
+    auto release_unit = [&](int ui) {
+        if (P.unit_jobs) sm::mbar_arrive(&rempty[ui % kRing]);
+    };
+
     if (warp == 0) {
         // ------------------------------------------------------------ producer
         if (lane == 0) {
             long long it = 0;
-            for (int j = jb0; j < jb1; ++j) {
+            for (int ui = 0;; ++ui) {
+            int j0u, j1u;
+            if (P.unit_jobs) {
+                const int sl = ui % kRing;
+                if (!sm::mbar_wait(&rempty[sl], (unsigned)(((ui / kRing) & 1) ^ 1), P.status, 18)) break;
+                const int u = atomicAdd(P.unit_counter, 1);
+                ring[sl] = u < P.nunits ? u : -1;
+                sm::mbar_arrive(&rfull[sl]);
+                if (u >= P.nunits) break;
+                const int2 r = P.unit_jobs[u];
+                j0u = r.x; j1u = r.x + r.y;
+            } else {
+                if (ui > 0) break;
+                j0u = jb0; j1u = jb1;
+            }
+            for (int j = j0u; j < j1u; ++j) {
                 const Job jb = P.jobs[j];
                 const bf16* bh = P.b_hi[jb.which & 1];
                 const bf16* bl = P.b_lo[jb.which & 1];
@@ -226,6 +281,7 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     sm::bulk_g2s(dst + 2 * CHUNK_A + CHUNK_B, bl + boff, CHUNK_B, &full[s]);
                 }
             }
+            }
         producer_done:;
         }
     } else if (warp == 1) {
@@ -233,10 +289,14 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         if (lane == 0) {
             long long it = 0;
             int lt = 0;
-            for (int j = jb0; j < jb1; ++j, ++lt) {
+            bool alive = true;
+            for (int ui = 0; alive; ++ui) {
+            int j0u, j1u;
+            if (!take_unit(ui, j0u, j1u)) break;
+            for (int j = j0u; j < j1u; ++j, ++lt) {
                 const int acc = lt & 1;
                 const unsigned aph = (unsigned)((lt >> 1) & 1);
-                if (!sm::mbar_wait(&acce[acc], aph ^ 1u, P.status, 12)) break;
+                if (!sm::mbar_wait(&acce[acc], aph ^ 1u, P.status, 12)) { alive = false; break; }
                 sm::tc_fence_after();
                 const uint32_t dt = tmem_base + (uint32_t)(acc * TC);
                 bool ok = true;
@@ -258,8 +318,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     }
                     sm::mma_commit(&empty[s]);
                 }
-                if (!ok) break;
+                if (!ok) { alive = false; break; }
                 sm::mma_commit(&accf[acc]);
+            }
+            release_unit(ui);
             }
             sm::mma_commit(done);
             sm::mbar_wait(done, 0, P.status, 14);
@@ -270,14 +332,20 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         // in tile order by build_records_kernel) into the free record buffer.
         if (MODE == MODE_SWEEP && lane == 0) {
             int lt = 0;
-            for (int j = jb0; j < jb1; ++j, ++lt) {
-                const Job jb = P.jobs[j];
-                const int acc = lt & 1;
-                const unsigned aph = (unsigned)((lt >> 1) & 1);
-                if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) break;
-                sm::mbar_arrive_expect_tx(&recf[acc], (unsigned)(RT * sizeof(float)));
-                sm::bulk_g2s(recs + (size_t)acc * RT, P.rec[jb.which & 1] + (size_t)jb.ctile * RT,
-                             (unsigned)(RT * sizeof(float)), &recf[acc]);
+            bool alive = true;
+            for (int ui = 0; alive; ++ui) {
+                int j0u, j1u;
+                if (!take_unit(ui, j0u, j1u)) break;
+                for (int j = j0u; j < j1u; ++j, ++lt) {
+                    const Job jb = P.jobs[j];
+                    const int acc = lt & 1;
+                    const unsigned aph = (unsigned)((lt >> 1) & 1);
+                    if (!sm::mbar_wait(&rece[acc], aph ^ 1u, P.status, 16)) { alive = false; break; }
+                    sm::mbar_arrive_expect_tx(&recf[acc], (unsigned)(RT * sizeof(float)));
+                    sm::bulk_g2s(recs + (size_t)acc * RT, P.rec[jb.which & 1] + (size_t)jb.ctile * RT,
+                                 (unsigned)(RT * sizeof(float)), &recf[acc]);
+                }
+                release_unit(ui);
             }
         }
     } else {
@@ -319,7 +387,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         for (int c = 0; c < kMaxD; ++c) nxq[c] = 0.f;
         const float dd = (float)P.d;
         const float ced2 = (dd + 2.f) * 5.97e-8f;
-        for (int j = jb0; j < jb1; ++j, ++lt) {
+        bool alive = true;
+        for (int ui = 0; alive; ++ui) {
+        int j0u, j1u;
+        if (!take_unit(ui, j0u, j1u)) break;
+        for (int j = j0u; j < j1u; ++j, ++lt) {
             const Job jb = P.jobs[j];
             const int acc = lt & 1;
             const unsigned aph = (unsigned)((lt >> 1) & 1);
@@ -351,11 +423,35 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 thr_keep = 0.f;   // tau2 = 1: keep everything
                 thr_heap = 0.f;   // and heap every pair whose |rho| bound is positive
             }
-            if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) break;
-            if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) break;
+            if (MODE == MODE_SWEEP && !sm::mbar_wait(&recf[acc], aph, P.status, 17)) { alive = false; break; }
+            if (!sm::mbar_wait(&accf[acc], aph, P.status, 15)) { alive = false; break; }
             sm::tc_fence_after();
             const float* rb = recs + (size_t)acc * RT;
-            const float* gtab = rb + TC * REC;  // group records of the tile
+            const float* gtab = rb + TC * REC + 2 * HBOX;  // group records of the tile
+            // kmax: an upper bound of the kernel value phase 1 computes for this row and any
+            // candidate of its half tile.  The half tile's box gives the smallest squared
+            // scaled distance dmin; phase 1's f32 distance (rounded differences, FMA chain) is
+            // at least dmin (1 - 1e-5), and its __expf / Matern polynomial stay within the
+            // relative margins below.
+            float kmax = 0.f;
+            if (MODE == MODE_SWEEP && qid >= 0) {
+                const float* hb = rb + TC * REC + half * HBOX;
+                float dmin = 0.f;
+#pragma unroll
+                for (int c = 0; c < DP; ++c) {
+                    const float a = hb[c] + nxq[c];      // lo_c - x_q,c
+                    const float b = hb[8 + c] + nxq[c];  // hi_c - x_q,c
+                    const float t = fmaxf(fmaxf(a, -b), 0.f);
+                    dmin = fmaf(t, t, dmin);
+                }
+                dmin *= (1.f - 1e-5f);
+                if (KT == 0) {
+                    kmax = P.var * __expf(-0.5f * dmin) * (1.f + 1e-5f);
+                } else {
+                    const float a0 = 2.2360679775f * sqrtf(dmin);
+                    kmax = P.var * (1.f + a0 + a0 * a0 * 0.33333334f) * __expf(-a0) * (1.f + 2e-5f);
+                }
+            }
             const bool keep_job = !(jb.which & 2);
             const bool feed_heap = !(jb.which & 4);
             const bool fast_ids = (jb.which & 8) != 0;
@@ -390,43 +486,20 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     continue;
                 }
                 if (qid < 0) continue;
-                // Group test: one certified bound for the group's 8 pairs.  The group record
-                // holds the box of the 8 candidates' scaled coordinates, their largest
-                // err_coef |v_c| and 1/sqrt(p_c).  The box's nearest and farthest points give
-                // bounds Kmax >= kv >= Kmin of the kernel value phase 1 would compute (its
-                // f32 coordinate distance, __expf and Matern polynomial, within the relative
-                // margins), so |kv - s| <= max(Kmax - s, s - Kmin) and phase 1's survivor
-                // bound is at most hi.  hi < thr_keep (<= thr_heap) means no pair of the group
-                // is kept or heaped: the group is done without phase 1.  Where the kernel
-                // value is negligible (candidates far from the query in coordinates) this
-                // skips the per-pair work; padding groups (NaN 1/sqrt(p)) always skip.
+                // Group test: one certified bound for the group's 8 pairs.  kmax bounds the
+                // kernel value phase 1 would compute for any candidate of the thread's half tile
+                // (from the half tile's coordinate box, once per job), so |kv - s| <=
+                // max(kmax - s, s) and phase 1's survivor bound of each pair is at most ghi (with
+                // the group's largest error term and 1/sqrt(p)).  ghi < thr_keep (<= thr_heap)
+                // means no pair of the group is kept or heaped: the group is done without phase
+                // 1.  It skips the per-pair work where the kernel value is negligible (candidates
+                // far from the query in coordinates); padding groups (NaN 1/sqrt(p)) always skip.
                 {
                     const float* gr = gtab + (size_t)(col0 >> 3) * GREC;
-                    float dmin = 0.f, dmax = 0.f;
-#pragma unroll
-                    for (int c = 0; c < DP; ++c) {
-                        const float a = gr[c] + nxq[c];      // lo_c - x_q,c
-                        const float b = gr[8 + c] + nxq[c];  // hi_c - x_q,c
-                        const float t = fmaxf(fmaxf(a, -b), 0.f);
-                        dmin = fmaf(t, t, dmin);
-                        const float u = fmaxf(fabsf(a), fabsf(b));
-                        dmax = fmaf(u, u, dmax);
-                    }
-                    dmin *= (1.f - 1e-5f);
-                    dmax *= (1.f + 1e-5f);
-                    float kmax, kmin;
-                    if (KT == 0) {
-                        kmax = P.var * __expf(-0.5f * dmin) * (1.f + 1e-5f);
-                        kmin = P.var * __expf(-0.5f * dmax) * (1.f - 1e-5f);
-                    } else {
-                        const float a0 = 2.2360679775f * sqrtf(dmin), a1 = 2.2360679775f * sqrtf(dmax);
-                        kmax = P.var * (1.f + a0 + a0 * a0 * 0.33333334f) * __expf(-a0) * (1.f + 2e-5f);
-                        kmin = P.var * (1.f + a1 + a1 * a1 * 0.33333334f) * __expf(-a1) * (1.f - 2e-5f);
-                    }
                     float rmax = 0.f;
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) rmax = fmaxf(rmax, fmaxf(kmax - v[i], v[i] - kmin));
-                    const float ghi = (rmax * (1.f + 3e-7f) + vnq * gr[16] + ekmax + 1e-30f) * gr[17] * (1.f + 1e-6f);
+                    for (int i = 0; i < 8; ++i) rmax = fmaxf(rmax, fmaxf(kmax - v[i], v[i]));
+                    const float ghi = (rmax * (1.f + 3e-7f) + vnq * gr[0] + ekmax + 1e-30f) * gr[1] * (1.f + 1e-6f);
                     if (!(ghi >= thr_keep)) continue;
                 }
                 // Phase 1, no stores: certified bounds of the group's 8 pairs, as
@@ -544,6 +617,9 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                 if (MODE == MODE_SWEEP) sm::mbar_arrive(&rece[acc]);
             }
         }
+        __syncwarp();
+        if (lane == 0) release_unit(ui);
+        }
         if (MODE == MODE_SWEEP && slot >= 0) P.surv_cnt[2 * slot + half] = cnt;
     }
     sm::tc_fence_before();
@@ -582,42 +658,44 @@ __global__ void build_records_kernel(const int* __restrict__ ids, long long rows
     }
 }
 
-// Group records of the sweep's group test, one per 8 consecutive candidates of a tile
-// (after the tile's candidate records): the box of their scaled coordinates (lo in
-// floats 0-7, hi in 8-15; 0 past d), the largest err_coef |v| (16) and 1/sqrt(p) (17).
-// A group without a valid row gets an empty box (+inf, -inf) and NaN 1/sqrt(p).
+// Half-tile boxes and group scalars of the sweep's group test (after a tile's candidate
+// records): one thread per half tile writes the box of its 128 candidates' scaled
+// coordinates (lo in floats 0-7, hi in 8-15; 0 past d; an empty box +inf / -inf when no
+// row is valid) and, for each of its 16 groups of 8, the largest err_coef |v| and the
+// largest 1/sqrt(p) (NaN when the group has no valid row).
 __global__ void build_group_records_kernel(const int* __restrict__ ids, long long rows, const float* __restrict__ xs,
                                            int d, const float* __restrict__ vn, const float* __restrict__ isp,
                                            float err_coef, float* __restrict__ rec) {
-    const long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (gi >= rows / 8) return;
-    const long long tile = gi / (TC / 8);
-    const int g = (int)(gi - tile * (TC / 8));
+    const long long hi_ = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (hi_ >= rows / (TC / 2)) return;
+    const long long tile = hi_ / 2;
+    const int h = (int)(hi_ - tile * 2);
     float lo[kMaxD], hi[kMaxD];
 #pragma unroll
     for (int c = 0; c < kMaxD; ++c) { lo[c] = __int_as_float(0x7f800000); hi[c] = -__int_as_float(0x7f800000); }
-    float emax = 0.f, imax = __int_as_float(0x7fc00000);
-    bool any = false;
-    for (int e = 0; e < 8; ++e) {
-        const int cid = ids[tile * TC + 8 * g + e];
-        if (cid < 0) continue;
+    float* base = rec + tile * RT + TC * REC;
+    for (int g = 0; g < TC / 16; ++g) {
+        float emax = 0.f, imax = __int_as_float(0x7fc00000);
+        bool any = false;
+        for (int e = 0; e < 8; ++e) {
+            const int cid = ids[tile * TC + h * (TC / 2) + 8 * g + e];
+            if (cid < 0) continue;
 #pragma unroll
-        for (int c = 0; c < kMaxD; ++c) {
-            const float x = c < d ? xs[(size_t)cid * d + c] : 0.f;
-            lo[c] = fminf(lo[c], x);
-            hi[c] = fmaxf(hi[c], x);
+            for (int c = 0; c < kMaxD; ++c) {
+                const float x = c < d ? xs[(size_t)cid * d + c] : 0.f;
+                lo[c] = fminf(lo[c], x);
+                hi[c] = fmaxf(hi[c], x);
+            }
+            emax = fmaxf(emax, err_coef * vn[cid]);
+            imax = any ? fmaxf(imax, isp[cid]) : isp[cid];
+            any = true;
         }
-        emax = fmaxf(emax, err_coef * vn[cid]);
-        imax = any ? fmaxf(imax, isp[cid]) : isp[cid];
-        any = true;
+        float* o = base + 2 * HBOX + (size_t)(h * (TC / 16) + g) * GREC;
+        o[0] = emax;
+        o[1] = imax;
     }
-    float* o = rec + tile * RT + TC * REC + (size_t)g * GREC;
 #pragma unroll
-    for (int c = 0; c < kMaxD; ++c) { o[c] = lo[c]; o[8 + c] = hi[c]; }
-    o[16] = emax;
-    o[17] = imax;
-    o[18] = 0.f;
-    o[19] = 0.f;
+    for (int c = 0; c < kMaxD; ++c) { base[h * HBOX + c] = lo[c]; base[h * HBOX + 8 + c] = hi[c]; }
 }
 
 // hi/lo split of V rows into the blocked layout.  rowmap[r] = dataset row of
@@ -1587,7 +1665,8 @@ static int pick_stages(int k) {
     return 0;
 }
 
-// ncta CTAs, CTA c runs jobs [cta_begin[c], cta_begin[c+1]).
+// ncta persistent CTAs: each claims units (dynamic schedule) or runs jobs
+// [cta_job_begin[c], cta_job_begin[c+1]) (static schedule, the diagnostic launch).
 static cudaError_t launch_sweep(const MMAParams& P, int mode, int ncta, cudaStream_t st) {
     if (ncta <= 0) return cudaSuccess;
     const size_t smem = smem_layout(P.k, P.nstages).total;
@@ -1711,10 +1790,10 @@ static int screen_prepare(ct_tree* T, cudaStream_t st) {
                                                                     S->isp, S->xmax, ec, S->rec_ds);
         build_records_kernel<<<grid_for(S->lvl_rows), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs, T->d, S->vn,
                                                                     S->isp, S->xmax, ec, S->rec_lvl);
-        build_group_records_kernel<<<grid_for(S->rows_pad / 8), 256, 0, st>>>(S->b_id_ds, S->rows_pad, T->xs, T->d,
-                                                                             S->vn, S->isp, ec, S->rec_ds);
-        build_group_records_kernel<<<grid_for(S->lvl_rows / 8), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs, T->d,
-                                                                              S->vn, S->isp, ec, S->rec_lvl);
+        build_group_records_kernel<<<grid_for(S->rows_pad / (TC / 2)), 256, 0, st>>>(S->b_id_ds, S->rows_pad, T->xs,
+                                                                                    T->d, S->vn, S->isp, ec, S->rec_ds);
+        build_group_records_kernel<<<grid_for(S->lvl_rows / (TC / 2)), 256, 0, st>>>(S->lvl_id, S->lvl_rows, T->xs,
+                                                                                     T->d, S->vn, S->isp, ec, S->rec_lvl);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
@@ -1762,7 +1841,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     int *a_slot_lvl = nullptr, *rowmap_lvl = nullptr;
     int *a_slot_x = nullptr, *rowmap_x = nullptr, *slot_id_x = nullptr;  // part-expanded (parts > 1)
     bf16 *al_hi = nullptr, *al_lo = nullptr;
-    int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr, *cta_begin = nullptr;
+    int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr, *unit_counter = nullptr;
+    int2* unit_jobs_d = nullptr;
     long long* part_idx = nullptr;
     float* part_dist = nullptr;
     long long* evals_d = nullptr;
@@ -1919,36 +1999,22 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             units.push_back(u);
         }
     }
-    // longest-processing-time assignment of units to persistent CTAs
+    // Units are claimed dynamically by the persistent CTAs, largest first (a list
+    // schedule in longest-processing-time order): a CTA whose units run fast takes more.
     std::vector<int> order(units.size());
     for (size_t i = 0; i < units.size(); ++i) order[i] = (int)i;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return units[a].count > units[b].count; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return units[a].count > units[b].count; });
     const int ncta = (int)std::min<long long>((long long)sms, (long long)order.size());
-    std::vector<std::vector<int>> per_cta(ncta);
-    std::vector<std::pair<long long, int>> load;  // (jobs, cta) min-heap
-    for (int c = 0; c < ncta; ++c) load.push_back({0, c});
-    auto cmp = [](const std::pair<long long, int>& a, const std::pair<long long, int>& b) { return a.first > b.first; };
-    std::make_heap(load.begin(), load.end(), cmp);
-    for (int u : order) {
-        std::pop_heap(load.begin(), load.end(), cmp);
-        auto& lc = load.back();
-        per_cta[lc.second].push_back(u);
-        lc.first += units[u].count;
-        std::push_heap(load.begin(), load.end(), cmp);
-    }
     std::vector<JobUnit> flat_units;
-    std::vector<int> begin(ncta + 1, 0);
+    std::vector<int2> unit_jobs_h;
     long long njobs = 0;
-    for (int c = 0; c < ncta; ++c) {
-        begin[c] = (int)njobs;
-        for (int u : per_cta[c]) {
-            JobUnit x = units[u];
-            x.off = njobs;
-            njobs += x.count;
-            flat_units.push_back(x);
-        }
+    for (int u : order) {
+        JobUnit x = units[u];
+        x.off = njobs;
+        unit_jobs_h.push_back(make_int2((int)njobs, x.count));
+        njobs += x.count;
+        flat_units.push_back(x);
     }
-    begin[ncta] = (int)njobs;
     const long long pairs_main = njobs * TQ * TC;  // every job runs its MMAs
     // part-expanded slots and A rows, the A operand, survivor lists
     const int* a_slot_use = a_slot_lvl;
@@ -1974,7 +2040,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     A((void**)&full_list, sizeof(int) * nslots);
     A((void**)&jobs, sizeof(Job) * (njobs + 1));
     A((void**)&units_d, sizeof(JobUnit) * (flat_units.size() + 1));
-    A((void**)&cta_begin, sizeof(int) * (ncta + 1));
+    A((void**)&unit_jobs_d, sizeof(int2) * (unit_jobs_h.size() + 1));
+    A((void**)&unit_counter, sizeof(int));
     if (e != cudaSuccess) return set_err(CT_ERR_NOMEM, "screened form allocation: %s", cudaGetErrorString(e));
     split_blocked_kernel<<<152 * 8, 256, 0, st>>>(vnat, m, rowmap_use, rows_x, al_hi, al_lo);
     ++launches;
@@ -1986,7 +2053,9 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             ++launches;
         }
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(cta_begin, begin.data(), sizeof(int) * (ncta + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !unit_jobs_h.empty())
+        e = cudaMemcpyAsync(unit_jobs_d, unit_jobs_h.data(), sizeof(int2) * unit_jobs_h.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(unit_counter, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(surv_cnt, 0, sizeof(int) * 2 * nslots, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(nfull_d, 0, sizeof(int), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(evals_d, 0, sizeof(long long), st);
@@ -1998,7 +2067,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     P.a_hi = al_hi; P.a_lo = al_lo; P.a_groups = rows_x / 8;
     P.b_hi[0] = S->lvl_hi; P.b_lo[0] = S->lvl_lo; P.b_groups[0] = S->lvl_rows / 8; P.b_id[0] = S->lvl_id;
     P.b_hi[1] = S->ds_hi; P.b_lo[1] = S->ds_lo; P.b_groups[1] = S->rows_pad / 8; P.b_id[1] = S->b_id_ds;
-    P.m = m; P.jobs = jobs; P.cta_job_begin = cta_begin;
+    P.m = m; P.jobs = jobs; P.cta_job_begin = nullptr;
+    P.unit_jobs = unit_jobs_d; P.nunits = (int)unit_jobs_h.size(); P.unit_counter = unit_counter;
     P.a_slot = a_slot_use; P.slot_id = slot_id_use;
     P.xs = xs; P.d = d; P.vn = S->vn; P.isp = S->isp; P.xmax = S->xmax;
     P.var = var; P.kernel_type = kernel_type; P.predecessor = predecessor ? 1 : 0;
@@ -2158,7 +2228,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     cudaFreeAsync(al_hi, st); cudaFreeAsync(al_lo, st);
     cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
-    cudaFreeAsync(jobs, st); cudaFreeAsync(cta_begin, st); cudaFreeAsync(qtau, st);
+    cudaFreeAsync(jobs, st); cudaFreeAsync(unit_jobs_d, st); cudaFreeAsync(unit_counter, st); cudaFreeAsync(qtau, st);
     if (units_d) cudaFreeAsync(units_d, st);
     if (a_slot_x) cudaFreeAsync(a_slot_x, st);
     if (rowmap_x) cudaFreeAsync(rowmap_x, st);

@@ -224,40 +224,34 @@ def _query_consts(q, data):
     return ekmax
 
 
-def group_hi(q, cands, data, v_mmas, kpick):
+def group_hi(q, half, cands, data, v_mmas, kpick):
     """The sweep epilogue's group test (screen_sweep_kernel), float32 operation by operation:
-    a bound on phase 1's survivor bound bhi of every pair of the group.  kpick selects
-    __expf at either end of its error band for Kmax (low end) and Kmin (high end)."""
+    kmax from the box of the half tile `half` (computed once per job), then a bound on
+    phase 1's survivor bound bhi of every pair of the group `cands` (a subset of the half
+    tile).  kpick 1 takes __expf at the low end of its error band."""
     Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
     u2 = 1.0 / 65536.0
     err_coef = F(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22)
-    lo = xs[cands].min(axis=0)
-    hi = xs[cands].max(axis=0)
+    lo = xs[half].min(axis=0)
+    hi = xs[half].max(axis=0)
     err_max = max(F(err_coef * vn[c]) for c in cands)
     isc_max = max(isp[c] for c in cands)
     dmin = F(0.0)
-    dmax = F(0.0)
     for a_ in range(d):
         a = F(lo[a_] + F(-xs[q, a_]))
         b = F(hi[a_] + F(-xs[q, a_]))
         t = max(max(a, F(-b)), F(0.0))
         dmin = fma32(t, t, dmin)
-        u = max(abs(a), abs(b))
-        dmax = fma32(u, u, dmax)
     dmin = F(dmin * F(1.0 - 1e-5))
-    dmax = F(dmax * F(1.0 + 1e-5))
-    lo_e, hi_e = (1, 2) if kpick else (0, 0)
+    lo_e = 1 if kpick else 0
     if kt == 0:
         kmax = F(F(F(var) * expf_band(F(F(-0.5) * dmin))[lo_e]) * F(1.0 + 1e-5))
-        kmin = F(F(F(var) * expf_band(F(F(-0.5) * dmax))[hi_e]) * F(1.0 - 1e-5))
     else:
         a0 = F(F(2.2360679775) * F(np.sqrt(dmin)))
-        a1 = F(F(2.2360679775) * F(np.sqrt(dmax)))
         kmax = F(F(F(F(var) * F(F(F(1.0) + a0) + F(F(a0 * a0) * F(0.33333334)))) * expf_band(F(-a0))[lo_e]) * F(1.0 + 2e-5))
-        kmin = F(F(F(F(var) * F(F(F(1.0) + a1) + F(F(a1 * a1) * F(0.33333334)))) * expf_band(F(-a1))[hi_e]) * F(1.0 - 2e-5))
     rmax = F(0.0)
     for v in v_mmas:
-        rmax = max(rmax, max(F(kmax - v), F(v - kmin)))
+        rmax = max(rmax, max(F(kmax - v), v))
     ekmax = _query_consts(q, data)
     inner = F(F(F(rmax * F(1.0 + 3e-7)) + F(vn[q] * err_max)) + F(ekmax + F(1e-30)))
     return F(F(inner * isc_max) * F(1.0 + 1e-6))
@@ -274,20 +268,22 @@ def test_group_test_bounds_every_pair(n, d, m, kt, ls):
     or heap: its bound is >= phase 1's survivor bound bhi of every pair, for tensor-core dots
     anywhere in the certified band, __expf at either end of its band, for groups of 8 points
     close together (coordinate-sorted, tight boxes), random groups, groups holding the query
-    itself and groups with tiny-p rows."""
+    itself and groups with tiny-p rows.  The kernel-value bound comes from the box of the
+    group's half tile (128 candidates)."""
     X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m + 5)
     xs, vn = data[1], data[2]
     u2 = 1.0 / 65536.0
     c_split = 3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22
     r = np.random.default_rng(23)
-    order = np.lexsort(tuple(xs[:, a] for a in range(d)))  # coordinate-sorted: neighbours in groups of 8
-    groups = [order[8 * g:8 * g + 8] for g in r.choice(n // 8, 12, replace=False)]
-    groups += [r.choice(n, 8, replace=False) for _ in range(8)]
-    groups += [np.concatenate([idx[:2], r.choice(n, 6, replace=False)])]
+    order = np.lexsort(tuple(xs[:, a] for a in range(d)))  # coordinate-sorted: tight half tiles
+    halves = [order[128 * h:128 * h + 128] for h in r.choice(n // 128, 6, replace=False)]
+    halves += [r.choice(n, 128, replace=False) for _ in range(3)]
+    halves += [np.concatenate([idx[:2], r.choice(n, 126, replace=False)])]
     queries = list(r.choice(n, 6, replace=False)) + [int(idx[0])]
     for q in queries:
-        gq = groups + [np.concatenate([[q], r.choice(n, 7, replace=False)])]
-        for cands in gq:
+        hq = halves + [np.concatenate([[q], r.choice(n, 127, replace=False)])]
+        for half in hq:
+          for cands in (half[:8], half[8:16], half[-8:]):
             cands = [int(c) for c in cands]
             for shift in (-1.0, 0.0, 1.0):
                 v_mmas = []
@@ -295,7 +291,7 @@ def test_group_test_bounds_every_pair(n, d, m, kt, ls):
                     exact = float(np.dot(V[q].astype(np.float64), V[c].astype(np.float64)))
                     v_mmas.append(F(exact + shift * c_split * float(vn[q]) * float(vn[c])))
                 for kpick in (0, 1):
-                    g = group_hi(q, cands, data, v_mmas, kpick)
+                    g = group_hi(q, half, cands, data, v_mmas, kpick)
                     for c, v in zip(cands, v_mmas):
                         if c == q:
                             continue  # the query itself: phase 1 marks it +inf (never rejected, see below)

@@ -1199,13 +1199,6 @@ __global__ void rescore_kernel(RescoreParams P) {
     if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)nk);
 }
 
-// Exhaustive rescoring of overflowed queries, split for parallelism: each warp
-// scores one chunk of a query's candidate range (P.chunk ids, sized to the work so
-// that a few overflowed queries still spread over the SMs) and keeps its k best keys.
-struct ChunkItem {
-    int slot, chunk;
-};
-
 __device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& fill, int k, bool has,
                                                  unsigned long long key) {
     const int lane = threadIdx.x & 31;
@@ -1221,50 +1214,6 @@ __device__ __forceinline__ void warp_topk_append(unsigned long long* keys, int& 
     if (has) keys[fill + __popc(mask & ((1u << lane) - 1u))] = key;
     fill += added;
     __syncwarp();
-}
-
-// Warp w scores item perm[w]: items are visited chunk-major, so the warps in flight
-// stream the same candidate rows; results land at the item's slot-major index.
-__global__ void rescore_chunk_kernel(RescoreParams P, const ChunkItem* items, const int* perm, int nitems,
-                                     unsigned long long* partial) {
-    extern __shared__ unsigned long long ckeys_all[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wpb = blockDim.x / 32;
-    unsigned long long* keys = ckeys_all + (size_t)warp * RBUF;
-    const long long w = (long long)blockIdx.x * wpb + warp;
-    if (w >= nitems) return;
-    const int wi = perm[w];
-    const ChunkItem it = items[wi];
-    const int q = P.slot_id[it.slot];
-    const int k = P.k;
-    float vql[32];
-    load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
-    for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
-    __syncwarp();
-    const long long count = P.predecessor ? (long long)q : P.n;
-    const long long b0 = (long long)it.chunk * P.chunk;
-    const long long b1 = b0 + P.chunk < count ? b0 + P.chunk : count;
-    int fill = k;
-    for (long long base = b0; base < b1; base += 32) {
-        const int nb = (int)((b1 - base) < 32 ? (b1 - base) : 32);
-        const int cid = lane < nb ? (int)(base + lane) : -1;
-        df mydot = df{0.f, 0.f};
-        for (int t = 0; t < nb; t += 4) {
-            int cc[4];
-            df dots[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) cc[u] = (t + u) < nb ? (int)(base + t + u) : -1;
-            warp_dots<4>(P.v, P.m, cc, vql, dots);
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (lane == t + u) mydot = dots[u];
-        }
-        const float dist = lane < nb ? exact_from_dot(P, q, cid, mydot) : 0.f;
-        warp_topk_append(keys, fill, k, lane < nb, pack_key(dist, cid));
-    }
-    warp_bitonic_sort(keys, sort_len(fill));
-    for (int j = lane; j < k; j += 32) partial[(size_t)wi * k + j] = keys[j];
-    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)(b1 - b0));
 }
 
 // Merge the chunk results of each overflowed query into its output row.
@@ -1388,60 +1337,155 @@ __device__ __forceinline__ int spiral_tile(const JobUnit& U, int w) {
     return right > left ? U.cc + (w - mm) : U.cc - (w - mm);
 }
 
-// Exhaustive rescoring of an overflowed part slot over its own candidates only: the
-// part's share of its query tile's list (spiral entries p, p + parts, ... of the
-// level tiles, then the dataset tiles), tpc tiles per item.  The part's exact top k
-// then joins the other parts' lists in the k-way merge.
-struct PartItem {
-    int slot, unit, j0;
+// Exhaustive rescoring, tiled: a CTA takes a group of up to XQ overflowed query slots
+// that share a candidate source (the main pass: the id range [0, cend); the part pass:
+// the tiles of one (query tile, part) unit) and one chunk of that source.  Candidate
+// rows are staged XC at a time in shared memory, transposed (element-major), so that
+// every staged row serves all the group's queries: lane l of warp w forms the
+// compensated dot products of candidate l with queries w and w + 8 (two interleaved
+// TwoProd/TwoSum accumulators per pair, combined in double-float), then the exact
+// distance and a streaming top-k per query.  Compared with one warp per (query,
+// chunk), the L2 traffic of the candidate rows falls by the group size.  Each slot's
+// partial top k of the chunk lands in its row of `partial`.
+constexpr int XQ = 16;    // query slots per group (two per warp)
+constexpr int XC = 32;    // candidates staged per block (one per lane)
+constexpr int XKB = 128;  // key buffer per query (k <= 64)
+struct ExhGroup {
+    int g0, ng;       // slots full_slots[g0 .. g0 + ng)
+    int unit;         // part pass: unit; main pass: -1
+    int nchunks;
+    long long cend;   // main pass: candidate ids [0, cend)
 };
-__global__ void rescore_part_kernel(RescoreParams P, const PartItem* __restrict__ items, int nitems, int tpc,
-                                    const JobUnit* __restrict__ units, const int* __restrict__ lvl_id,
-                                    const int* __restrict__ ds_id, unsigned long long* __restrict__ partial) {
-    extern __shared__ unsigned long long pkeys_all[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned long long* keys = pkeys_all + (size_t)warp * RBUF;
-    const long long w = (long long)blockIdx.x * (blockDim.x >> 5) + warp;
-    if (w >= nitems) return;
-    const PartItem it = items[w];
-    const JobUnit U = units[it.unit];
-    const int q = P.slot_id[it.slot];
-    const int k = P.k;
-    float vql[32];
-    load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
-    for (int i = lane; i < RBUF; i += 32) keys[i] = ~0ULL;
-    __syncwarp();
-    const int mine = U.count - U.warm;
-    const int j1 = it.j0 + tpc < mine ? it.j0 + tpc : mine;
-    int fill = k;
-    long long evals = 0;
-    for (int j = it.j0; j < j1; ++j) {
-        const int wt = U.p + j * U.parts;
-        const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
-                                    : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
-        for (int base = 0; base < TC; base += 32) {
-            int cid = ids[base + lane];
-            if (P.predecessor && cid >= q) cid = -1;
-            df mydot = df{0.f, 0.f};
-            for (int t = 0; t < 32; t += 4) {
-                int cc[4];
-                df dots[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) cc[u] = __shfl_sync(0xffffffffu, cid, t + u);
-                warp_dots<4>(P.v, P.m, cc, vql, dots);
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (lane == t + u) mydot = dots[u];
-            }
-            const bool has = cid >= 0;
-            const float dist = has ? exact_from_dot(P, q, cid, mydot) : 0.f;
-            evals += __popc(__ballot_sync(0xffffffffu, has));
-            warp_topk_append(keys, fill, k, has, pack_key(dist, cid));
-        }
+struct ExhItem {
+    int group, chunk;
+};
+__host__ __device__ inline size_t tile_smem_bytes(int m) {
+    return sizeof(float) * (size_t)m * XC + sizeof(float) * (size_t)XQ * m + sizeof(unsigned long long) * XQ * XKB;
+}
+
+__device__ __forceinline__ void keys_append(unsigned long long* keys, int& fill, int k, bool has,
+                                            unsigned long long key) {
+    const int lane = threadIdx.x & 31;
+    const unsigned mask = __ballot_sync(0xffffffffu, has);
+    const int added = __popc(mask);
+    if (fill + added > XKB) {
+        __syncwarp();
+        warp_bitonic_sort(keys, XKB);
+        for (int i = k + lane; i < XKB; i += 32) keys[i] = ~0ULL;
+        __syncwarp();
+        fill = k;
     }
-    warp_bitonic_sort(keys, sort_len(fill));
-    for (int j = lane; j < k; j += 32) partial[(size_t)w * k + j] = keys[j];
-    if (lane == 0 && P.evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
+    if (has) keys[fill + __popc(mask & ((1u << lane) - 1u))] = key;
+    fill += added;
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, const ExhGroup* __restrict__ groups,
+                                                           const ExhItem* __restrict__ items, const int* __restrict__ ibeg,
+                                                           int cand_chunk, int tpc, const JobUnit* __restrict__ units,
+                                                           const int* __restrict__ lvl_id, const int* __restrict__ ds_id,
+                                                           unsigned long long* __restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char xs_raw[];
+    const int m = P.m, k = P.k;
+    float* cs = (float*)xs_raw;                                            // [m][XC]
+    float* qs = cs + (size_t)m * XC;                                       // [XQ][m]
+    unsigned long long* kb = (unsigned long long*)(qs + (size_t)XQ * m);  // [XQ][XKB]
+    __shared__ int cid_s[XC];
+    __shared__ int qid_s[XQ];
+    const ExhItem it = items[blockIdx.x];
+    const ExhGroup G = groups[it.group];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < XQ) qid_s[threadIdx.x] = threadIdx.x < G.ng ? P.slot_id[P.full_slots[G.g0 + threadIdx.x]] : -1;
+    __syncthreads();
+    for (int e = threadIdx.x; e < XQ * m; e += blockDim.x) {
+        const int g = e / m;
+        const int q = qid_s[g];
+        qs[e] = q >= 0 ? P.v[(size_t)q * m + (e - g * m)] : 0.f;
+    }
+    for (int e = threadIdx.x; e < XQ * XKB; e += blockDim.x) kb[e] = ~0ULL;
+    long long c_lo = 0, total = 0;
+    int t_lo = 0;
+    JobUnit U{};
+    if (G.unit < 0) {
+        c_lo = (long long)it.chunk * cand_chunk;
+        const long long c_hi = G.cend < c_lo + cand_chunk ? G.cend : c_lo + cand_chunk;
+        total = c_hi > c_lo ? c_hi - c_lo : 0;
+    } else {
+        U = units[G.unit];
+        const int mine = U.count - U.warm;
+        t_lo = it.chunk * tpc;
+        const int t_hi = mine < t_lo + tpc ? mine : t_lo + tpc;
+        total = t_hi > t_lo ? (long long)(t_hi - t_lo) * TC : 0;
+    }
+    const int ga = warp, gb = warp + 8;
+    const int ida = qid_s[ga], idb = qid_s[gb];
+    unsigned long long* ka = kb + (size_t)ga * XKB;
+    unsigned long long* kbb = kb + (size_t)gb * XKB;
+    const float* qa = qs + (size_t)ga * m;
+    const float* qb = qs + (size_t)gb * m;
+    int fa = k, fb = k;
+    long long evals = 0;
+    __syncthreads();
+    for (long long b0 = 0; b0 < total; b0 += XC) {
+        if (threadIdx.x < XC) {
+            const long long o = b0 + threadIdx.x;
+            int cid = -1;
+            if (o < total) {
+                if (G.unit < 0) {
+                    cid = (int)(c_lo + o);
+                } else {
+                    const int j = t_lo + (int)(o / TC);
+                    const int wt = U.p + j * U.parts;
+                    const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                                                : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
+                    cid = ids[o % TC];
+                }
+            }
+            cid_s[threadIdx.x] = cid;
+        }
+        __syncthreads();
+        // stage: thread t moves float4 (t / XC) of row (t % XC); the transposed stores of a
+        // warp fall in 32 different banks
+        for (int t = threadIdx.x; t < XC * (m >> 2); t += blockDim.x) {
+            const int r = t % XC, j = t / XC;
+            const int cid = cid_s[r];
+            const float4 x = cid >= 0 ? __ldg((const float4*)(P.v + (size_t)cid * m) + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+            cs[(4 * j + 0) * XC + r] = x.x;
+            cs[(4 * j + 1) * XC + r] = x.y;
+            cs[(4 * j + 2) * XC + r] = x.z;
+            cs[(4 * j + 3) * XC + r] = x.w;
+        }
+        __syncthreads();
+        const int cid = cid_s[lane];
+        float sa0 = 0.f, ca0 = 0.f, sa1 = 0.f, ca1 = 0.f, sb0 = 0.f, cb0 = 0.f, sb1 = 0.f, cb1 = 0.f;
+#pragma unroll 4
+        for (int e = 0; e < m; e += 2) {
+            const float x0 = cs[e * XC + lane], x1 = cs[(e + 1) * XC + lane];
+            const float2 a = *(const float2*)(qa + e);
+            const float2 b = *(const float2*)(qb + e);
+            two_sum_acc(sa0, ca0, a.x, x0);
+            two_sum_acc(sa1, ca1, a.y, x1);
+            two_sum_acc(sb0, cb0, b.x, x0);
+            two_sum_acc(sb1, cb1, b.y, x1);
+        }
+        const df da = df_add(df_two_sum(sa0, ca0), df_two_sum(sa1, ca1));
+        const df db = df_add(df_two_sum(sb0, cb0), df_two_sum(sb1, cb1));
+        const bool va = ida >= 0 && cid >= 0 && (!P.predecessor || cid < ida);
+        const bool vb = idb >= 0 && cid >= 0 && (!P.predecessor || cid < idb);
+        const float dista = va ? exact_from_dot(P, ida, cid, da) : 0.f;
+        const float distb = vb ? exact_from_dot(P, idb, cid, db) : 0.f;
+        evals += __popc(__ballot_sync(0xffffffffu, va)) + __popc(__ballot_sync(0xffffffffu, vb));
+        keys_append(ka, fa, k, va, pack_key(dista, cid));
+        keys_append(kbb, fb, k, vb, pack_key(distb, cid));
+        __syncthreads();
+    }
+    warp_bitonic_sort(ka, XKB);
+    warp_bitonic_sort(kbb, XKB);
+    if (ga < G.ng)
+        for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0 + ga] + it.chunk) * k + j] = ka[j];
+    if (gb < G.ng)
+        for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0 + gb] + it.chunk) * k + j] = kbb[j];
+    if (lane == 0 && P.evals && evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
 }
 
 // Job i of a unit: i < warm: warm-up (heap only) over the part's i-th level tile;
@@ -2105,15 +2149,14 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nfull, nfull_d, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, S->status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    ChunkItem* items_d = nullptr;
-    PartItem* pitems_d = nullptr;
+    ExhGroup* groups_d = nullptr;
+    ExhItem* xitems_d = nullptr;
     int* item_begin_d = nullptr;
-    int* perm_d = nullptr;
     unsigned long long* partial = nullptr;
     if (e == cudaSuccess && nfull > 0) {
-        // Split every overflowed slot's exhaustive range into items, about 24 warps'
-        // worth per SM in all (at most 4096 candidates per item).
-        const long long target_items = (long long)sms * 24;
+        // Group the overflowed slots that share a candidate source (XQ per group) and
+        // split each group's source into chunks, about six CTAs' worth per SM in all.
+        const long long target_items = (long long)sms * 6;
         std::vector<int> fl(nfull), sid(nslots);
         e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id_use, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st);
@@ -2123,75 +2166,78 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             if (e == cudaSuccess) e = cudaMemcpyAsync(sorted_q.data(), val_lvl, sizeof(int) * nq, cudaMemcpyDeviceToHost, st);
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        std::sort(fl.begin(), fl.end());
+        std::vector<ExhGroup> groups;
         std::vector<int> ibeg(nfull + 1, 0);
-        int nitems = 0;
-        std::vector<ChunkItem> items;
-        std::vector<PartItem> pitems;
-        std::vector<int> perm;
-        int tpc = 1;
+        int tpc = 1, cand_chunk = 4096;
         if (parts > 1) {
             // slot s*parts + pp of query s: its A tile, then the unit (tile, part)
             std::vector<int> tile_of(nq, -1), unit_of(nqt * parts, -1);
             for (long long r = 0; r < nq; ++r) tile_of[sorted_q[r]] = (int)(r / TQ);
             for (size_t u = 0; u < flat_units.size(); ++u) unit_of[flat_units[u].qx] = (int)u;
-            long long total_tiles = 0;
-            std::vector<int> fu(nfull, -1);
+            std::vector<std::pair<int, int>> su(nfull);  // (unit, slot)
             for (int i = 0; i < nfull; ++i) {
                 const int qi = fl[i] / parts, pp = fl[i] % parts;
-                fu[i] = unit_of[(long long)tile_of[qi] * parts + pp];
-                if (fu[i] >= 0) total_tiles += flat_units[fu[i]].count - flat_units[fu[i]].warm;
+                su[i] = {unit_of[(long long)tile_of[qi] * parts + pp], fl[i]};
             }
-            tpc = (int)std::min<long long>(16, std::max<long long>(1, (total_tiles + target_items - 1) / target_items));
-            exh_pairs = total_tiles * TC;
-            for (int i = 0; i < nfull; ++i) {
-                ibeg[i] = (int)pitems.size();
-                if (fu[i] < 0) continue;
-                const int mine = flat_units[fu[i]].count - flat_units[fu[i]].warm;
-                for (int j0 = 0; j0 < mine; j0 += tpc) pitems.push_back(PartItem{fl[i], fu[i], j0});
+            std::sort(su.begin(), su.end());
+            for (int i = 0; i < nfull; ++i) fl[i] = su[i].second;
+            long long group_tiles = 0;
+            for (int i = 0; i < nfull;) {
+                int j = i;
+                while (j < nfull && j - i < XQ && su[j].first == su[i].first) ++j;
+                const int u = su[i].first;
+                const int mine = u >= 0 ? flat_units[u].count - flat_units[u].warm : 0;
+                groups.push_back(ExhGroup{i, j - i, u, 0, 0});
+                group_tiles += mine;
+                if (u >= 0) exh_pairs += (long long)mine * TC * (j - i);
+                i = j;
             }
-            ibeg[nfull] = (int)pitems.size();
-            nitems = (int)pitems.size();
+            tpc = (int)std::min<long long>(16, std::max<long long>(1, (group_tiles + target_items - 1) / target_items));
+            for (auto& g : groups) {
+                const int mine = g.unit >= 0 ? flat_units[g.unit].count - flat_units[g.unit].warm : 0;
+                g.nchunks = (mine + tpc - 1) / tpc;
+            }
         } else {
-            long long total = 0;
-            for (int i = 0; i < nfull; ++i) total += predecessor ? (long long)sid[fl[i]] : n;
-            exh_pairs = total;
-            R.chunk = (int)std::min<long long>(4096, std::max<long long>(256, ((total + target_items - 1) / target_items + 255) / 256 * 256));
-            for (int i = 0; i < nfull; ++i) {
-                ibeg[i] = (int)items.size();
-                const long long count = predecessor ? (long long)sid[fl[i]] : n;
-                for (long long c = 0; c * R.chunk < count; ++c) items.push_back(ChunkItem{fl[i], (int)c});
+            std::sort(fl.begin(), fl.end(), [&](int a, int b) { return sid[a] < sid[b] || (sid[a] == sid[b] && a < b); });
+            long long group_cands = 0;
+            for (int i = 0; i < nfull; i += XQ) {
+                const int j = std::min(nfull, i + XQ);
+                const long long cend = predecessor ? (long long)sid[fl[j - 1]] : n;
+                groups.push_back(ExhGroup{i, j - i, -1, 0, cend});
+                group_cands += cend;
+                for (int t = i; t < j; ++t) exh_pairs += predecessor ? (long long)sid[fl[t]] : n;
             }
-            ibeg[nfull] = (int)items.size();
-            nitems = (int)items.size();
-            perm.resize(nitems);
-            for (int i = 0; i < nitems; ++i) perm[i] = i;
-            std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return items[a].chunk < items[b].chunk; });
+            cand_chunk = (int)std::min<long long>(16384, std::max<long long>(1024, ((group_cands + target_items - 1) / target_items + 255) / 256 * 256));
+            for (auto& g : groups) g.nchunks = (int)((g.cend + cand_chunk - 1) / cand_chunk);
         }
+        int rows = 0;
+        std::vector<ExhItem> xitems;
+        for (size_t gi = 0; gi < groups.size(); ++gi) {
+            const ExhGroup& g = groups[gi];
+            for (int t = g.g0; t < g.g0 + g.ng; ++t) { ibeg[t] = rows; rows += g.nchunks; }
+            for (int c = 0; c < g.nchunks; ++c) xitems.push_back(ExhItem{(int)gi, c});
+        }
+        ibeg[nfull] = rows;
+        // chunk-major: CTAs in flight read the same candidate rows
+        std::stable_sort(xitems.begin(), xitems.end(), [](const ExhItem& a, const ExhItem& b) { return a.chunk < b.chunk; });
+        const int nitems = (int)xitems.size();
         A((void**)&item_begin_d, sizeof(int) * (nfull + 1));
-        A((void**)&partial, sizeof(unsigned long long) * ((size_t)nitems * k + 1));
-        if (parts > 1) {
-            A((void**)&pitems_d, sizeof(PartItem) * (nitems + 1));
-            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(pitems_d, pitems.data(), sizeof(PartItem) * nitems, cudaMemcpyHostToDevice, st);
-        } else {
-            A((void**)&items_d, sizeof(ChunkItem) * (nitems + 1));
-            A((void**)&perm_d, sizeof(int) * (nitems + 1));
-            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(items_d, items.data(), sizeof(ChunkItem) * nitems, cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess && nitems > 0) e = cudaMemcpyAsync(perm_d, perm.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, st);
-        }
+        A((void**)&partial, sizeof(unsigned long long) * ((size_t)rows * k + 1));
+        A((void**)&groups_d, sizeof(ExhGroup) * (groups.size() + 1));
+        A((void**)&xitems_d, sizeof(ExhItem) * (nitems + 1));
+        if (e == cudaSuccess && !groups.empty())
+            e = cudaMemcpyAsync(groups_d, groups.data(), sizeof(ExhGroup) * groups.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && nitems > 0)
+            e = cudaMemcpyAsync(xitems_d, xitems.data(), sizeof(ExhItem) * nitems, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, st);
         R.nfull = nfull;
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_chunk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_part_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        const size_t tsmem = tile_smem_bytes(m);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(merge_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (e == cudaSuccess && nitems > 0) {
-            const unsigned grid = (unsigned)((nitems + rwpb - 1) / rwpb);
-            if (parts > 1)
-                rescore_part_kernel<<<grid, 32 * rwpb, rsmem, st>>>(R, pitems_d, nitems, tpc, units_d, S->lvl_id,
-                                                                   S->b_id_ds, partial);
-            else
-                rescore_chunk_kernel<<<grid, 32 * rwpb, rsmem, st>>>(R, items_d, perm_d, nitems, partial);
+            rescore_tile_kernel<<<(unsigned)nitems, 256, tsmem, st>>>(R, groups_d, xitems_d, item_begin_d, cand_chunk, tpc,
+                                                                       units_d, S->lvl_id, S->b_id_ds, partial);
             merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, item_begin_d, partial);
             e = cudaGetLastError();
             launches += 2;
@@ -2235,9 +2281,8 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     if (slot_id_x) cudaFreeAsync(slot_id_x, st);
     if (part_idx) cudaFreeAsync(part_idx, st);
     if (part_dist) cudaFreeAsync(part_dist, st);
-    if (items_d) cudaFreeAsync(items_d, st);
-    if (pitems_d) cudaFreeAsync(pitems_d, st);
-    if (perm_d) cudaFreeAsync(perm_d, st);
+    if (groups_d) cudaFreeAsync(groups_d, st);
+    if (xitems_d) cudaFreeAsync(xitems_d, st);
     if (item_begin_d) cudaFreeAsync(item_begin_d, st);
     if (partial) cudaFreeAsync(partial, st);
     if (e != cudaSuccess) return set_err(CT_ERR_CUDA, "screened form: %s", cudaGetErrorString(e));

@@ -37,6 +37,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <type_traits>
+#include <tuple>
 #include <vector>
 
 #include "ct_common.cuh"
@@ -71,6 +72,9 @@ constexpr int GREC = 2;                     // floats per group of 8 candidates
 constexpr int RT = TC * REC + 2 * HBOX + (TC / 8) * GREC;  // floats of one candidate tile's records
 constexpr int kSurvCap = 1024;  // survivors per query slot (two column halves), at most RBUF
 constexpr int RBUF = 1024;                  // rescoring sort buffer (power of two)
+// Overflowed query slots with |v_q| / sqrt(p_q) up to this go to the filtered exhaustive
+// pass (certified FP32 bounds first); above it the bounds exclude almost nothing.
+constexpr float kFilterIsq = 256.f;
 static_assert(kSurvCap <= RBUF, "a slot's survivors must fit the rescoring buffer");
 
 enum Mode { MODE_DEBUG = 0, MODE_SWEEP = 1 };
@@ -797,6 +801,7 @@ struct RescoreParams {
     const float* xmax;           // max |x / l| per row
     const unsigned* xmax_max;    // bits of the dataset's largest xmax
     const unsigned* isp_max;     // bits of the dataset's largest 1 / sqrt(p)
+    const unsigned* qtau;        // per query (slot / parts): the sweep's smallest part threshold (d^2 bits)
 };
 
 // ---------------------------------------------------------- double-float
@@ -878,14 +883,15 @@ __device__ __forceinline__ df df_exp(df x) {
 // splits a row of m <= 1024 floats into 32 lane slices of m/32 contiguous
 // elements (4-float aligned when m % 128 == 0, else scalar); each lane keeps
 // the query slice in registers and accumulates a (sum, compensation) pair.
+// (explicitly rounded operations: no contraction, the same result at every call site)
 __device__ __forceinline__ void two_sum_acc(float& s, float& comp, float a, float b) {
-    const float pr = a * b;
-    const float pe = fmaf(a, b, -pr);
-    const float ts = s + pr;
-    const float z = ts - s;
-    const float se = (s - (ts - z)) + (pr - z);
+    const float pr = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -pr);
+    const float ts = __fadd_rn(s, pr);
+    const float z = __fsub_rn(ts, s);
+    const float se = __fadd_rn(__fsub_rn(s, __fsub_rn(ts, z)), __fsub_rn(pr, z));
     s = ts;
-    comp += se + pe;
+    comp = __fadd_rn(comp, __fadd_rn(se, pe));
 }
 
 // Load the query slice: lane l holds elements [l*m/32, (l+1)*m/32).
@@ -897,7 +903,20 @@ __device__ __forceinline__ void load_query_slice(const float* row, int m, float 
     for (int t = 0; t < 32; ++t) vq[t] = t < per ? r[t] : 0.f;
 }
 
+// One step of the warp reduction of (sum, compensation) pairs: TwoSum of the sums, the
+// compensations added.  Symmetric in its arguments, so both lanes of a butterfly pair
+// end with the same value.
+__device__ __forceinline__ void df_combine(float& hi, float& lo, float oh, float ol) {
+    const float t = __fadd_rn(hi, oh);
+    const float z = __fsub_rn(t, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(oh, z));
+    hi = t;
+    lo = __fadd_rn(__fadd_rn(lo, ol), err);
+}
+
 // Dots of the query slice with NC candidate rows at once (independent loads in flight).
+// Lane L sums elements [L m/32, (L+1) m/32) in order; the lanes' pairs are combined by a
+// butterfly over lane offsets 16, 8, 4, 2, 1.
 template <int NC>
 __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, const int (&cid)[NC],
                                           const float (&vq)[32], df (&out)[NC]) {
@@ -945,11 +964,7 @@ __device__ __forceinline__ void warp_dots(const float* __restrict__ V, int m, co
         for (int off = 16; off > 0; off >>= 1) {
             const float oh = __shfl_xor_sync(0xffffffffu, hi, off);
             const float ol = __shfl_xor_sync(0xffffffffu, lo, off);
-            const float t = hi + oh;
-            const float z = t - hi;
-            const float err = (hi - (t - z)) + (oh - z);
-            hi = t;
-            lo = (lo + ol) + err;
+            df_combine(hi, lo, oh, ol);
         }
         out[c] = df_fast(hi, lo);
     }
@@ -1041,11 +1056,13 @@ __device__ __forceinline__ void warp_dots_f32(const float* __restrict__ V, int m
 // Certified bounds [dl2, du2] of d^2 = 1 - |rho| for one pair from an FP32 dot with
 // error <= ed: the kernel value from the scaled f32 coordinates with the sweep's error
 // model (ale, bee, alk, bek as there), the normalisation 1 / sqrt(max(p_q p_c, 1e-18)).
-__device__ __forceinline__ void pair_bounds_f32(const RescoreParams& P, int q, int c, float dot, float ed, float isq,
-                                                float alk, float bek, float ale, float bee, float& dl2, float& du2) {
+// xq, xc: the pair's scaled coordinates (global or shared memory); isc = 1 / sqrt(p_c).
+__device__ __forceinline__ void pair_bounds_core(const RescoreParams& P, const float* xq, const float* xc, float isc,
+                                                 float dot, float ed, float isq, float alk, float bek, float ale,
+                                                 float bee, float& dl2, float& du2) {
     float d2 = 0.f;
     for (int a = 0; a < P.d; ++a) {
-        const float t = __fsub_rn(P.xs[(size_t)c * P.d + a], P.xs[(size_t)q * P.d + a]);
+        const float t = __fsub_rn(xc[a], xq[a]);
         d2 = __fmaf_rn(t, t, d2);
     }
     float kv, ek;
@@ -1061,11 +1078,16 @@ __device__ __forceinline__ void pair_bounds_f32(const RescoreParams& P, int q, i
     }
     const float R = fabsf(__fsub_rn(kv, dot));
     const float e = __fadd_rn(__fadd_rn(ed, ek), __fmaf_rn(R, 1.2e-7f, 1e-30f));
-    const float sc = fminf(__fmul_rn(isq, P.isp[c]), 1e9f);
+    const float sc = fminf(__fmul_rn(isq, isc), 1e9f);
     const float rl = __fmul_rn(__fmul_rn(fmaxf(__fsub_rn(R, e), 0.f), sc), 1.f - 2e-6f);
     const float rh = __fmul_rn(__fmul_rn(__fadd_rn(R, e), sc), 1.f + 2e-6f);
     du2 = 1.f - fminf(rl, 1.f);
     dl2 = fmaxf(1.f - fminf(rh, 1.f), 0.f);
+}
+__device__ __forceinline__ void pair_bounds_f32(const RescoreParams& P, int q, int c, float dot, float ed, float isq,
+                                                float alk, float bek, float ale, float bee, float& dl2, float& du2) {
+    pair_bounds_core(P, P.xs + (size_t)q * P.d, P.xs + (size_t)c * P.d, P.isp[c], dot, ed, isq, alk, bek, ale, bee,
+                     dl2, du2);
 }
 
 // Survivor rescoring, one warp per query slot, in two steps.
@@ -1244,11 +1266,18 @@ __global__ void merge_chunks_kernel(RescoreParams P, const int* item_begin, cons
     }
 }
 
+// Slots whose survivor lists overflowed; bit 31 marks those for the filtered pass.
 __global__ void collect_overflow_kernel(const int* __restrict__ surv_cnt, long long nslots, int half_cap,
-                                        int* __restrict__ list, int* __restrict__ nlist) {
+                                        const int* __restrict__ slot_id, const float* __restrict__ isp,
+                                        const float* __restrict__ vn, int filter, int* __restrict__ list,
+                                        int* __restrict__ nlist) {
     long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= nslots) return;
-    if (surv_cnt[2 * s] > half_cap || surv_cnt[2 * s + 1] > half_cap) list[atomicAdd(nlist, 1)] = (int)s;
+    if (surv_cnt[2 * s] > half_cap || surv_cnt[2 * s + 1] > half_cap) {
+        const int q = slot_id[s];
+        const bool f = filter && q >= 0 && isp[q] * vn[q] <= kFilterIsq;
+        list[atomicAdd(nlist, 1)] = (int)s | (f ? (int)0x80000000u : 0);
+    }
 }
 
 
@@ -1380,6 +1409,7 @@ __device__ __forceinline__ void keys_append(unsigned long long* keys, int& fill,
     __syncwarp();
 }
 
+template <int PER>  // m / 32 when fixed at compile time (8 or 16), else 0
 __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, const ExhGroup* __restrict__ groups,
                                                            const ExhItem* __restrict__ items, const int* __restrict__ ibeg,
                                                            int cand_chunk, int tpc, const JobUnit* __restrict__ units,
@@ -1392,6 +1422,7 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
     unsigned long long* kb = (unsigned long long*)(qs + (size_t)XQ * m);  // [XQ][XKB]
     __shared__ int cid_s[XC];
     __shared__ int qid_s[XQ];
+    const int per = PER > 0 ? PER : m >> 5;
     const ExhItem it = items[blockIdx.x];
     const ExhGroup G = groups[it.group];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1457,21 +1488,58 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
         }
         __syncthreads();
         const int cid = cid_s[lane];
-        float sa0 = 0.f, ca0 = 0.f, sa1 = 0.f, ca1 = 0.f, sb0 = 0.f, cb0 = 0.f, sb1 = 0.f, cb1 = 0.f;
-#pragma unroll 4
-        for (int e = 0; e < m; e += 2) {
-            const float x0 = cs[e * XC + lane], x1 = cs[(e + 1) * XC + lane];
-            const float2 a = *(const float2*)(qa + e);
-            const float2 b = *(const float2*)(qb + e);
-            two_sum_acc(sa0, ca0, a.x, x0);
-            two_sum_acc(sa1, ca1, a.y, x1);
-            two_sum_acc(sb0, cb0, b.x, x0);
-            two_sum_acc(sb1, cb1, b.y, x1);
-        }
-        const df da = df_add(df_two_sum(sa0, ca0), df_two_sum(sa1, ca1));
-        const df db = df_add(df_two_sum(sb0, cb0), df_two_sum(sb1, cb1));
         const bool va = ida >= 0 && cid >= 0 && (!P.predecessor || cid < ida);
         const bool vb = idb >= 0 && cid >= 0 && (!P.predecessor || cid < idb);
+        // The dot in warp_dots' order, so that a pair's exact distance is the same whichever
+        // pass scores it: 32 segments of m/32 elements, each summed in order, combined as
+        // the butterfly does (lane offsets 16, 8, 4, 2, 1).  Taking segment rev5(c) at step
+        // c turns that tree into a binary counter: pend[L] holds the finished subtree of
+        // 2^L segments while bit L of c is set.
+        float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
+        float pend[5][4];
+#pragma unroll
+        for (int L = 0; L < 5; ++L) pend[L][0] = pend[L][1] = pend[L][2] = pend[L][3] = 0.f;
+        for (int c = 0; c < 32; ++c) {
+            const int seg = (int)(__brev((unsigned)c) >> 27);
+            const float* qas = qa + seg * per;
+            const float* qbs = qb + seg * per;
+            const float* css = cs + (size_t)seg * per * XC + lane;
+            ha = 0.f; la = 0.f; hb = 0.f; lb = 0.f;
+            if (PER > 0) {
+#pragma unroll
+                for (int t4 = 0; t4 < PER; t4 += 4) {
+                    const float4 a4 = *(const float4*)(qas + t4);
+                    const float4 b4 = *(const float4*)(qbs + t4);
+                    const float x0 = css[(t4 + 0) * XC], x1 = css[(t4 + 1) * XC];
+                    const float x2 = css[(t4 + 2) * XC], x3 = css[(t4 + 3) * XC];
+                    two_sum_acc(ha, la, a4.x, x0); two_sum_acc(hb, lb, b4.x, x0);
+                    two_sum_acc(ha, la, a4.y, x1); two_sum_acc(hb, lb, b4.y, x1);
+                    two_sum_acc(ha, la, a4.z, x2); two_sum_acc(hb, lb, b4.z, x2);
+                    two_sum_acc(ha, la, a4.w, x3); two_sum_acc(hb, lb, b4.w, x3);
+                }
+            } else {
+                for (int t = 0; t < per; ++t) {
+                    const float x = css[t * XC];
+                    two_sum_acc(ha, la, qas[t], x);
+                    two_sum_acc(hb, lb, qbs[t], x);
+                }
+            }
+            bool placed = false;
+#pragma unroll
+            for (int L = 0; L < 5; ++L) {
+                if (!placed) {
+                    if ((c >> L) & 1) {
+                        df_combine(ha, la, pend[L][0], pend[L][1]);
+                        df_combine(hb, lb, pend[L][2], pend[L][3]);
+                    } else {
+                        pend[L][0] = ha; pend[L][1] = la; pend[L][2] = hb; pend[L][3] = lb;
+                        placed = true;
+                    }
+                }
+            }
+        }
+        const df da = df_fast(ha, la);
+        const df db = df_fast(hb, lb);
         const float dista = va ? exact_from_dot(P, ida, cid, da) : 0.f;
         const float distb = vb ? exact_from_dot(P, idb, cid, db) : 0.f;
         evals += __popc(__ballot_sync(0xffffffffu, va)) + __popc(__ballot_sync(0xffffffffu, vb));
@@ -1485,6 +1553,377 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
         for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0 + ga] + it.chunk) * k + j] = ka[j];
     if (gb < G.ng)
         for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0 + gb] + it.chunk) * k + j] = kbb[j];
+    if (lane == 0 && P.evals && evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
+}
+
+// Sparse plain slots: an overflowed slot of a tiny-p query whose candidate source no other
+// such slot shares (a small call's part slots) gets whole warps instead of a 16-row group:
+// warp per (slot, chunk) item, the survivor pass's warp dots on 32 candidates at a time,
+// exact distances lane-parallel, a streaming top-k buffer per warp.
+__global__ void __launch_bounds__(256) rescore_warp_kernel(RescoreParams P, const ExhGroup* __restrict__ groups,
+                                                           const ExhItem* __restrict__ items, int nitems,
+                                                           const int* __restrict__ ibeg, int cand_chunk, int tpc,
+                                                           const JobUnit* __restrict__ units,
+                                                           const int* __restrict__ lvl_id,
+                                                           const int* __restrict__ ds_id,
+                                                           unsigned long long* __restrict__ partial) {
+    __shared__ unsigned long long wkeys[8][XKB];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * 8 + warp;
+    if (w >= nitems) return;
+    const ExhItem it = items[w];
+    const ExhGroup G = groups[it.group];
+    const int m = P.m, k = P.k;
+    const int q = P.slot_id[P.full_slots[G.g0]];
+    unsigned long long* keys = wkeys[warp];
+    for (int i = lane; i < XKB; i += 32) keys[i] = ~0ULL;
+    __syncwarp();
+    long long c_lo = 0, total = 0;
+    int t_lo = 0;
+    JobUnit U{};
+    if (G.unit < 0) {
+        c_lo = (long long)it.chunk * cand_chunk;
+        const long long c_hi = G.cend < c_lo + cand_chunk ? G.cend : c_lo + cand_chunk;
+        total = c_hi > c_lo ? c_hi - c_lo : 0;
+    } else {
+        U = units[G.unit];
+        const int mine = U.count - U.warm;
+        t_lo = it.chunk * tpc;
+        const int t_hi = mine < t_lo + tpc ? mine : t_lo + tpc;
+        total = t_hi > t_lo ? (long long)(t_hi - t_lo) * TC : 0;
+    }
+    long long evals = 0;
+    if (q >= 0) {
+        float vql[32];
+        load_query_slice(P.v + (size_t)q * m, m, vql);
+        int fill = k;
+        for (long long b0 = 0; b0 < total; b0 += 32) {
+            const long long o = b0 + lane;
+            int cid = -1;
+            if (o < total) {
+                if (G.unit < 0) {
+                    cid = (int)(c_lo + o);
+                } else {
+                    const int wt = U.p + (t_lo + (int)(o / TC)) * U.parts;
+                    const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                                                : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
+                    cid = ids[o % TC];
+                }
+            }
+            const bool has = cid >= 0 && !(P.predecessor && cid >= q);
+            const unsigned hm = __ballot_sync(0xffffffffu, has);
+            if (hm == 0u) continue;
+            df mydot = df{0.f, 0.f};
+            for (int t = 0; t < 32; t += 4) {
+                if (((hm >> t) & 15u) == 0u) continue;
+                int cc[4];
+                df dd4[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int src = __shfl_sync(0xffffffffu, cid, t + u);
+                    cc[u] = (hm >> (t + u)) & 1u ? src : -1;
+                }
+                warp_dots<4>(P.v, m, cc, vql, dd4);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (lane == t + u) mydot = dd4[u];
+            }
+            const float dist = has ? exact_from_dot(P, q, cid, mydot) : 0.f;
+            evals += __popc(hm);
+            keys_append(keys, fill, k, has, pack_key(dist, cid));
+        }
+    }
+    __syncwarp();
+    warp_bitonic_sort(keys, XKB);
+    for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0] + it.chunk) * k + j] = keys[j];
+    if (lane == 0 && P.evals && evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
+}
+
+// ---------------------------------------------------------- filtered exhaustive pass
+// Overflowed slots whose residual variance is not tiny (|v_q| / sqrt(p_q) <= kFilterIsq)
+// are rescored over their whole candidate source, block by block of FCB = 256
+// candidates (one sweep tile), in two steps:
+//  F: an FP32 GEMM of the group's FQ = 4 QPT query rows against the block.  A thread
+//     holds QPT queries x 4 candidates; the block's rows are staged in K-chunks of 32 by
+//     16-byte cp.async into a double buffer.  Each dot is a blocked sum: FMA chains of
+//     FLB = 16 terms added into a running total, error <= (FLB + m / FLB + 1) 2^-24
+//     |v_q| |v_c| (half the survivor pass's four interleaved chains at m = 256).  The dots
+//     go to shared memory; the warp that owns a query row then bounds its 256 pairs
+//     (pair_bounds_core) and keeps those whose dl2 reaches the query's threshold tau^2:
+//     the query's shared threshold (seeded before the sweep, lowered by every part's
+//     heap), then the k-th exact distance seen here plus the seeds' margin for the
+//     double-float error.  A pair above tau^2 cannot enter the top k.
+//  E: the same warp rescores its kept pairs exactly with the survivor pass's warp dots
+//     (the same double-float value for a pair in either pass) into the query's streaming
+//     top-k buffer.
+// QPT = 8 serves groups of up to 32 slots, QPT = 4 groups of up to 16.
+constexpr int FCB = 256;      // candidates per block
+constexpr int FKC = 32;       // K-chunk per stage
+constexpr int FKP = FKC + 4;  // padded staged row (floats): conflict-free 16-byte reads
+constexpr int FLB = 16;       // FMA chain length per partial sum
+constexpr int FDP = FCB + 4;  // padded row of the dot matrix (floats)
+static_assert(FCB == TC, "a block of the filtered pass is one sweep tile");
+__host__ __device__ inline size_t filter_smem_bytes(int m, int qpt) {
+    const int fq = 4 * qpt, fqp = fq + 4;
+    return sizeof(float) * (2 * FCB * FKP + (size_t)m * fqp) + sizeof(unsigned long long) * fq * XKB + fq * FCB +
+           sizeof(float) * (FCB * 8 + 2 * FCB + fq * 16) + sizeof(int) * (FCB + 2 * fq);
+}
+
+__device__ __forceinline__ void cp_async16_zfill(void* smem_dst, const void* gsrc, int src_bytes) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gsrc), "r"(src_bytes) : "memory");
+}
+
+template <int QPT>
+__global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, const ExhGroup* __restrict__ groups,
+                                                             const ExhItem* __restrict__ items,
+                                                             const int* __restrict__ ibeg, int cand_chunk, int tpc,
+                                                             const JobUnit* __restrict__ units,
+                                                             const int* __restrict__ lvl_id,
+                                                             const int* __restrict__ ds_id,
+                                                             unsigned long long* __restrict__ partial) {
+    constexpr int FQ = 4 * QPT, FQP = FQ + 4, RPW = FQ / 8;  // query rows, padded row, rows per warp
+    static_assert(FQ * FDP <= 2 * FCB * FKP, "the dot matrix reuses the staging buffers");
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int m = P.m, k = P.k, d = P.d;
+    float* cbuf = (float*)fsm;                                                     // [2][FCB][FKP]
+    float* dots = cbuf;                                                            // [FQ][FDP] after the K loop
+    float* qsT = cbuf + 2 * FCB * FKP;                                             // [m][FQP]
+    unsigned long long* kb = (unsigned long long*)(qsT + (size_t)m * FQP);        // [FQ][XKB]
+    unsigned char* plist = (unsigned char*)(kb + FQ * XKB);                       // [FQ][FCB]
+    float* cx = (float*)(plist + FQ * FCB);                                        // [FCB][8]
+    float* cisp = cx + FCB * 8;
+    float* cvn = cisp + FCB;
+    float* qc = cvn + FCB;        // [FQ][8]: isq, ed / |v_c|, alk, bek, ale, bee, margin, tau^2
+    float* qx = qc + FQ * 8;      // [FQ][8]
+    int* cid_s = (int*)(qx + FQ * 8);
+    int* qid_s = cid_s + FCB;
+    const ExhItem it = items[blockIdx.x];
+    const ExhGroup G = groups[it.group];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid < FQ) {
+        const int q = tid < G.ng ? P.slot_id[P.full_slots[G.g0 + tid]] : -1;
+        qid_s[tid] = q;
+        float* c = qc + tid * 8;
+        if (q >= 0) {
+            const float dd = (float)d, ced2 = (dd + 2.f) * 5.97e-8f;
+            const float isq = P.isp[q];
+            const float A = 2.4e-7f * (P.xmax[q] + __uint_as_float(__ldg(P.xmax_max)));
+            c[0] = isq;
+            c[1] = (float)(FLB + m / FLB + 1) * 5.97e-8f * P.vn[q];
+            c[2] = (6e-8f + 0.5f * ced2 + 0.25f * A * dd) * 1.00001f;
+            c[3] = (1e-6f + 0.25f * A) * 1.00001f;
+            c[4] = (ced2 + 0.5f * A * dd) * 1.00001f;
+            c[5] = 0.5f * A * 1.00001f;
+            c[6] = 4e-12f * fminf(isq * __uint_as_float(__ldg(P.isp_max)) * 1.01f, 1e9f) + 1e-12f;
+            c[7] = fminf(1.f, __uint_as_float(P.qtau[P.full_slots[G.g0 + tid] / P.parts]));
+            for (int a = 0; a < d; ++a) qx[tid * 8 + a] = P.xs[(size_t)q * d + a];
+        } else {
+            c[7] = -1.f;
+        }
+    }
+    __syncthreads();
+    for (int e = tid; e < FQ * m; e += blockDim.x) {
+        const int g = e / m, kx = e - g * m;
+        const int q = qid_s[g];
+        qsT[(size_t)kx * FQP + g] = q >= 0 ? P.v[(size_t)q * m + kx] : 0.f;
+    }
+    for (int e = tid; e < FQ * XKB; e += blockDim.x) kb[e] = ~0ULL;
+    // the item's candidate blocks
+    long long c_lo = 0, total = 0;
+    int t_lo = 0, nblocks = 0;
+    JobUnit U{};
+    if (G.unit < 0) {
+        c_lo = (long long)it.chunk * cand_chunk;
+        const long long c_hi = G.cend < c_lo + cand_chunk ? G.cend : c_lo + cand_chunk;
+        total = c_hi > c_lo ? c_hi - c_lo : 0;
+        nblocks = (int)((total + FCB - 1) / FCB);
+    } else {
+        U = units[G.unit];
+        const int mine = U.count - U.warm;
+        t_lo = it.chunk * tpc;
+        const int t_hi = mine < t_lo + tpc ? mine : t_lo + tpc;
+        nblocks = t_hi > t_lo ? t_hi - t_lo : 0;
+    }
+    const int tq = warp >> 1;                    // queries QPT tq .. QPT tq + QPT - 1
+    const int tc = ((warp & 1) << 5) | lane;     // candidates tc + 64 j
+    const int nk = m / FKC;
+    int fill[RPW];
+#pragma unroll
+    for (int r = 0; r < RPW; ++r) fill[r] = k;
+    long long evals = 0;
+    for (int b = 0; b < nblocks; ++b) {
+        __syncthreads();  // the previous block's ids, rows and dots are no longer read
+        {
+            int cid = -1;
+            if (G.unit < 0) {
+                const long long o = (long long)b * FCB + tid;
+                if (o < total) cid = (int)(c_lo + o);
+            } else {
+                const int wt = U.p + (t_lo + b) * U.parts;
+                const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                                            : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
+                cid = ids[tid];
+            }
+            cid_s[tid] = cid;
+            if (cid >= 0) {
+                for (int a = 0; a < d; ++a) cx[tid * 8 + a] = P.xs[(size_t)cid * d + a];
+                cisp[tid] = P.isp[cid];
+                cvn[tid] = P.vn[cid];
+            }
+        }
+        __syncthreads();
+        auto stage = [&](int kc, int bf) {
+            float* dst = cbuf + bf * FCB * FKP;
+            const int piece = tid & 7;
+#pragma unroll
+            for (int i = 0; i < FCB / 32; ++i) {
+                const int r = (tid >> 3) + 32 * i;
+                const int cid = cid_s[r];
+                const float* src = P.v + (size_t)(cid >= 0 ? cid : 0) * m + kc * FKC + piece * 4;
+                cp_async16_zfill(dst + r * FKP + piece * 4, src, cid >= 0 ? 16 : 0);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        float tot[QPT][4];
+#pragma unroll
+        for (int i = 0; i < QPT; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) tot[i][j] = 0.f;
+        stage(0, 0);
+        for (int kc = 0; kc < nk; ++kc) {
+            if (kc + 1 < nk) {
+                stage(kc + 1, (kc + 1) & 1);
+                asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            } else {
+                asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            }
+            __syncthreads();
+            const float* cb = cbuf + (kc & 1) * FCB * FKP;
+            const float* qb = qsT + (size_t)kc * FKC * FQP + QPT * tq;
+#pragma unroll
+            for (int h = 0; h < FKC / FLB; ++h) {
+                float acc[QPT][4];
+#pragma unroll
+                for (int i = 0; i < QPT; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+#pragma unroll
+                for (int k4 = 0; k4 < FLB; k4 += 4) {
+                    const int kk = h * FLB + k4;
+                    float4 x[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) x[j] = *(const float4*)(cb + (tc + 64 * j) * FKP + kk);
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        float qv[QPT];
+#pragma unroll
+                        for (int i4 = 0; i4 < QPT; i4 += 4) {
+                            const float4 qa = *(const float4*)(qb + (kk + t) * FQP + i4);
+                            qv[i4] = qa.x; qv[i4 + 1] = qa.y; qv[i4 + 2] = qa.z; qv[i4 + 3] = qa.w;
+                        }
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const float xv = t == 0 ? x[j].x : t == 1 ? x[j].y : t == 2 ? x[j].z : x[j].w;
+#pragma unroll
+                            for (int i = 0; i < QPT; ++i) acc[i][j] = __fmaf_rn(qv[i], xv, acc[i][j]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < QPT; ++i)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) tot[i][j] = __fadd_rn(tot[i][j], acc[i][j]);
+            }
+            __syncthreads();  // buffer kc & 1 is free for chunk kc + 2 (and, at the end, for the dots)
+        }
+#pragma unroll
+        for (int i = 0; i < QPT; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dots[(QPT * tq + i) * FDP + tc + 64 * j] = tot[i][j];
+        __syncthreads();
+        // F bounds and E, warp w owns query rows w, w + 8, ...
+        for (int r = 0; r < RPW; ++r) {
+            const int ql = warp + 8 * r;
+            const int q = qid_s[ql];
+            if (q < 0) continue;
+            const float* c = qc + ql * 8;
+            const float tau2 = c[7];
+            int nkept = 0;
+            for (int c0 = 0; c0 < FCB; c0 += 32) {
+                const int cl = c0 + lane;
+                const int cid = cid_s[cl];
+                bool keep = cid >= 0 && !(P.predecessor && cid >= q);
+                if (keep && cid != q) {  // the query itself: d = 0
+                    float dl2, du2;
+                    pair_bounds_core(P, qx + ql * 8, cx + cl * 8, cisp[cl], dots[ql * FDP + cl],
+                                     __fmul_rn(c[1], cvn[cl]), c[0], c[2], c[3], c[4], c[5], dl2, du2);
+                    keep = dl2 <= tau2;
+                }
+                const unsigned mk = __ballot_sync(0xffffffffu, keep);
+                if (keep) plist[ql * FCB + nkept + __popc(mk & ((1u << lane) - 1u))] = (unsigned char)cl;
+                nkept += __popc(mk);
+            }
+            if (nkept == 0) continue;
+            __syncwarp();
+            unsigned long long* keys = kb + (size_t)ql * XKB;
+            float vql[32];
+            load_query_slice(P.v + (size_t)q * m, m, vql);
+            int fl = fill[0];
+#pragma unroll
+            for (int rr = 1; rr < RPW; ++rr)
+                if (r == rr) fl = fill[rr];
+            for (int base = 0; base < nkept; base += 32) {
+                const int ci = base + lane;
+                const bool has = ci < nkept;
+                const int cid = has ? cid_s[plist[ql * FCB + ci]] : -1;
+                const int nb = nkept - base < 32 ? nkept - base : 32;
+                df mydot = df{0.f, 0.f};
+                for (int t = 0; t < nb; t += 4) {
+                    int cc[4];
+                    df dd4[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int src = __shfl_sync(0xffffffffu, cid, (t + u) & 31);
+                        cc[u] = (t + u) < nb ? src : -1;
+                    }
+                    warp_dots<4>(P.v, m, cc, vql, dd4);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u)
+                        if (lane == t + u) mydot = dd4[u];
+                }
+                const float dist = has ? exact_from_dot(P, q, cid, mydot) : 0.f;
+                evals += nb;
+                keys_append(keys, fl, k, has, pack_key(dist, cid));
+            }
+            // every 16 new entries: sort, keep the k best, tighten tau^2 by the k-th
+            if (fl >= k + 16) {
+                __syncwarp();
+                warp_bitonic_sort(keys, XKB);
+                for (int i = k + lane; i < XKB; i += 32) keys[i] = ~0ULL;
+                fl = k;
+                __syncwarp();
+                const unsigned long long kk = keys[k - 1];
+                if (kk != ~0ULL) {
+                    const float dk = __uint_as_float((unsigned)(kk >> 32));
+                    const float t2 = __fadd_ru(__fmul_ru(__fmul_ru(dk, dk), 1.000004f), c[6]);
+                    __syncwarp();
+                    if (lane == 0) qc[ql * 8 + 7] = fminf(tau2, t2);
+                }
+            }
+#pragma unroll
+            for (int rr = 0; rr < RPW; ++rr)
+                if (r == rr) fill[rr] = fl;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < RPW; ++r) {
+        const int ql = warp + 8 * r;
+        unsigned long long* keys = kb + (size_t)ql * XKB;
+        warp_bitonic_sort(keys, XKB);
+        if (ql < G.ng)
+            for (int j = lane; j < k; j += 32) partial[((size_t)ibeg[G.g0 + ql] + it.chunk) * k + j] = keys[j];
+    }
     if (lane == 0 && P.evals && evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
 }
 
@@ -2132,119 +2571,238 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     R.k = k; R.evals = evals_d;
     R.order = val_lvl; R.parts = parts;
     R.xs = xs; R.vn = S->vn; R.isp = S->isp; R.xmax = S->xmax; R.xmax_max = S->xmax_max; R.isp_max = S->isp_max;
+    R.qtau = qtau;
     R.out_idx = parts > 1 ? part_idx : (long long*)out_idx;
     R.out_dist = parts > 1 ? part_dist : out_dist;
     const int rwpb = 8;
     const size_t rsmem = sizeof(unsigned long long) * RBUF * rwpb;
+    int smem_optin = 0;
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const size_t fsmem8 = filter_smem_bytes(m, 8), fsmem4 = filter_smem_bytes(m, 4);
+    const bool can_filter = m <= 1024 && fsmem8 <= (size_t)smem_optin;
     const size_t ssmem = (sizeof(unsigned long long) + sizeof(float)) * RBUF * rwpb;  // survivor pass
     if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ssmem);
-    if (e == cudaSuccess) {
-        rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, ssmem, st>>>(R);
-        collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, half_cap, full_list, nfull_d);
-        e = cudaGetLastError();
-        launches += 2;
-    }
+    // The overflow list first: the exhaustive pass is planned on the host and runs on side
+    // streams while the survivor pass runs on the call's stream.
     int nfull = 0, status = 0;
     long long exh_pairs = 0;  // candidates of the exhaustive pass (part tiles count whole tiles)
+    cudaEvent_t ev_ovf = nullptr;
+    if (e == cudaSuccess) {
+        collect_overflow_kernel<<<grid_for(nslots), 256, 0, st>>>(surv_cnt, nslots, half_cap, slot_id_use, S->isp, S->vn,
+                                                                    can_filter ? 1 : 0, full_list, nfull_d);
+        e = cudaGetLastError();
+        ++launches;
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(&nfull, nfull_d, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&status, S->status, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev_ovf, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev_ovf, st);
+    if (e == cudaSuccess) {
+        rescore_kernel<<<(unsigned)((nslots + rwpb - 1) / rwpb), 32 * rwpb, ssmem, st>>>(R);
+        e = cudaGetLastError();
+        ++launches;
+    }
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev_ovf);
     ExhGroup* groups_d = nullptr;
     ExhItem* xitems_d = nullptr;
     int* item_begin_d = nullptr;
     unsigned long long* partial = nullptr;
+    cudaStream_t aux[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev_aux[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     if (e == cudaSuccess && nfull > 0) {
-        // Group the overflowed slots that share a candidate source (XQ per group) and
-        // split each group's source into chunks, about six CTAs' worth per SM in all.
-        const long long target_items = (long long)sms * 6;
+        int prio = 0;
+        cudaStreamGetPriority(st, &prio);
+        for (auto& a : aux)
+            if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&a, cudaStreamNonBlocking, prio);
+        for (auto& v : ev_aux)
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming);
+        cudaStream_t x0 = aux[0];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(x0, ev_ovf, 0);
+        auto AX = [&](void** ptr, size_t bytes) { if (e == cudaSuccess) e = cudaMallocAsync(ptr, bytes ? bytes : 16, x0); };
+        // Group the overflowed slots that share a candidate source and split each group's
+        // source into chunks.  Four kinds: plain (tiny p; 5..XQ slots per group), filtered
+        // groups of 17..32 slots (QPT = 8) and of up to 16 (QPT = 4), and plain slots in
+        // groups of up to 4, split into one warp item per slot and chunk.
+        const long long target_items = (long long)sms * 4;
         std::vector<int> fl(nfull), sid(nslots);
-        e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id_use, sizeof(int) * nslots, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fl.data(), full_list, sizeof(int) * nfull, cudaMemcpyDeviceToHost, x0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(sid.data(), slot_id_use, sizeof(int) * nslots, cudaMemcpyDeviceToHost, x0);
         std::vector<int> sorted_q;
         if (parts > 1) {
             sorted_q.resize(nq);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(sorted_q.data(), val_lvl, sizeof(int) * nq, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(sorted_q.data(), val_lvl, sizeof(int) * nq, cudaMemcpyDeviceToHost, x0);
         }
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(x0);
+        // fl entries carry bit 31 for slots of the filtered pass until they are grouped
+        auto slot_of = [](int v) { return v & 0x7fffffff; };
+        auto filt_of = [](int v) { return v < 0 ? 1 : 0; };
         std::vector<ExhGroup> groups;
-        std::vector<int> ibeg(nfull + 1, 0);
-        int tpc = 1, cand_chunk = 4096;
+        std::vector<int> gkind;
+        auto kind_of = [](int f, int ng) { return f ? (ng > 16 ? 1 : 2) : (ng > 4 ? 0 : 3); };
+        auto add_group = [&](ExhGroup g, int kd) {  // a sparse plain group becomes one group per slot
+            if (kd == 3) {
+                for (int t = 0; t < g.ng; ++t) {
+                    groups.push_back(ExhGroup{g.g0 + t, 1, g.unit, 0, g.cend});
+                    gkind.push_back(3);
+                }
+            } else {
+                groups.push_back(g);
+                gkind.push_back(kd);
+            }
+        };
         if (parts > 1) {
             // slot s*parts + pp of query s: its A tile, then the unit (tile, part)
             std::vector<int> tile_of(nq, -1), unit_of(nqt * parts, -1);
             for (long long r = 0; r < nq; ++r) tile_of[sorted_q[r]] = (int)(r / TQ);
             for (size_t u = 0; u < flat_units.size(); ++u) unit_of[flat_units[u].qx] = (int)u;
-            std::vector<std::pair<int, int>> su(nfull);  // (unit, slot)
+            std::vector<std::tuple<int, int, int>> su(nfull);  // (unit, filtered, slot)
             for (int i = 0; i < nfull; ++i) {
-                const int qi = fl[i] / parts, pp = fl[i] % parts;
-                su[i] = {unit_of[(long long)tile_of[qi] * parts + pp], fl[i]};
+                const int sl = slot_of(fl[i]);
+                const int qi = sl / parts, pp = sl % parts;
+                su[i] = std::make_tuple(unit_of[(long long)tile_of[qi] * parts + pp], filt_of(fl[i]), sl);
             }
             std::sort(su.begin(), su.end());
-            for (int i = 0; i < nfull; ++i) fl[i] = su[i].second;
-            long long group_tiles = 0;
+            for (int i = 0; i < nfull; ++i) fl[i] = std::get<2>(su[i]);
             for (int i = 0; i < nfull;) {
+                const int u = std::get<0>(su[i]), f = std::get<1>(su[i]);
+                const int cap = f ? 32 : XQ;
                 int j = i;
-                while (j < nfull && j - i < XQ && su[j].first == su[i].first) ++j;
-                const int u = su[i].first;
+                while (j < nfull && j - i < cap && std::get<0>(su[j]) == u && std::get<1>(su[j]) == f) ++j;
                 const int mine = u >= 0 ? flat_units[u].count - flat_units[u].warm : 0;
-                groups.push_back(ExhGroup{i, j - i, u, 0, 0});
-                group_tiles += mine;
+                add_group(ExhGroup{i, j - i, u, 0, mine}, kind_of(f, j - i));  // cend: the source's tiles (for chunking)
                 if (u >= 0) exh_pairs += (long long)mine * TC * (j - i);
                 i = j;
             }
-            tpc = (int)std::min<long long>(16, std::max<long long>(1, (group_tiles + target_items - 1) / target_items));
-            for (auto& g : groups) {
-                const int mine = g.unit >= 0 ? flat_units[g.unit].count - flat_units[g.unit].warm : 0;
-                g.nchunks = (mine + tpc - 1) / tpc;
-            }
         } else {
-            std::sort(fl.begin(), fl.end(), [&](int a, int b) { return sid[a] < sid[b] || (sid[a] == sid[b] && a < b); });
-            long long group_cands = 0;
-            for (int i = 0; i < nfull; i += XQ) {
-                const int j = std::min(nfull, i + XQ);
-                const long long cend = predecessor ? (long long)sid[fl[j - 1]] : n;
-                groups.push_back(ExhGroup{i, j - i, -1, 0, cend});
-                group_cands += cend;
-                for (int t = i; t < j; ++t) exh_pairs += predecessor ? (long long)sid[fl[t]] : n;
+            std::sort(fl.begin(), fl.end(), [&](int a, int b) {
+                const int fa = filt_of(a), fb = filt_of(b), sa = slot_of(a), sb = slot_of(b);
+                if (fa != fb) return fa < fb;
+                return sid[sa] < sid[sb] || (sid[sa] == sid[sb] && sa < sb);
+            });
+            for (int i = 0; i < nfull;) {
+                const int f = filt_of(fl[i]);
+                const int cap = f ? 32 : XQ;
+                int j = i;
+                while (j < nfull && j - i < cap && filt_of(fl[j]) == f) ++j;
+                const long long cend = predecessor ? (long long)sid[slot_of(fl[j - 1])] : n;
+                add_group(ExhGroup{i, j - i, -1, 0, cend}, kind_of(f, j - i));
+                for (int t = i; t < j; ++t) exh_pairs += predecessor ? (long long)sid[slot_of(fl[t])] : n;
+                i = j;
             }
-            cand_chunk = (int)std::min<long long>(16384, std::max<long long>(1024, ((group_cands + target_items - 1) / target_items + 255) / 256 * 256));
-            for (auto& g : groups) g.nchunks = (int)((g.cend + cand_chunk - 1) / cand_chunk);
+            for (int i = 0; i < nfull; ++i) fl[i] = slot_of(fl[i]);
         }
+        // chunking per kind: about target_items CTAs each (warps for the warp items)
+        int ktpc[4] = {1, 1, 1, 1}, kchunk[4] = {4096, 4096, 4096, 4096};
+        for (int kd = 0; kd < 4; ++kd) {
+            long long work = 0;
+            for (size_t gi = 0; gi < groups.size(); ++gi)
+                if (gkind[gi] == kd) work += groups[gi].cend;
+            const long long target = kd == 3 ? target_items * 8 : target_items;
+            if (parts > 1)
+                ktpc[kd] = (int)std::min<long long>(16, std::max<long long>(1, (work + target - 1) / target));
+            else
+                kchunk[kd] = (int)std::min<long long>(
+                    16384, std::max<long long>(1024, ((work + target - 1) / target + 255) / 256 * 256));
+        }
+        for (size_t gi = 0; gi < groups.size(); ++gi) {
+            ExhGroup& g = groups[gi];
+            const int kd = gkind[gi];
+            if (parts > 1) {
+                g.nchunks = (int)((g.cend + ktpc[kd] - 1) / ktpc[kd]);
+                g.cend = 0;
+            } else {
+                g.nchunks = (int)((g.cend + kchunk[kd] - 1) / kchunk[kd]);
+            }
+        }
+        std::vector<int> ibeg(nfull + 1, 0);
         int rows = 0;
-        std::vector<ExhItem> xitems;
+        std::vector<ExhItem> kitems[4];
         for (size_t gi = 0; gi < groups.size(); ++gi) {
             const ExhGroup& g = groups[gi];
             for (int t = g.g0; t < g.g0 + g.ng; ++t) { ibeg[t] = rows; rows += g.nchunks; }
-            for (int c = 0; c < g.nchunks; ++c) xitems.push_back(ExhItem{(int)gi, c});
+            for (int c = 0; c < g.nchunks; ++c) kitems[gkind[gi]].push_back(ExhItem{(int)gi, c});
         }
         ibeg[nfull] = rows;
-        // chunk-major: CTAs in flight read the same candidate rows
-        std::stable_sort(xitems.begin(), xitems.end(), [](const ExhItem& a, const ExhItem& b) { return a.chunk < b.chunk; });
-        const int nitems = (int)xitems.size();
-        A((void**)&item_begin_d, sizeof(int) * (nfull + 1));
-        A((void**)&partial, sizeof(unsigned long long) * ((size_t)rows * k + 1));
-        A((void**)&groups_d, sizeof(ExhGroup) * (groups.size() + 1));
-        A((void**)&xitems_d, sizeof(ExhItem) * (nitems + 1));
+        // chunk-major within each kind: CTAs in flight read the same candidate rows
+        std::vector<ExhItem> xitems;
+        int koff[5] = {0, 0, 0, 0, 0};
+        for (int kd = 0; kd < 4; ++kd) {
+            std::stable_sort(kitems[kd].begin(), kitems[kd].end(),
+                             [](const ExhItem& a, const ExhItem& b) { return a.chunk < b.chunk; });
+            koff[kd] = (int)xitems.size();
+            xitems.insert(xitems.end(), kitems[kd].begin(), kitems[kd].end());
+        }
+        koff[4] = (int)xitems.size();
+        const int nitems = koff[4];
+        AX((void**)&item_begin_d, sizeof(int) * (nfull + 1));
+        AX((void**)&partial, sizeof(unsigned long long) * ((size_t)rows * k + 1));
+        AX((void**)&groups_d, sizeof(ExhGroup) * (groups.size() + 1));
+        AX((void**)&xitems_d, sizeof(ExhItem) * (nitems + 1));
         if (e == cudaSuccess && !groups.empty())
-            e = cudaMemcpyAsync(groups_d, groups.data(), sizeof(ExhGroup) * groups.size(), cudaMemcpyHostToDevice, st);
+            e = cudaMemcpyAsync(groups_d, groups.data(), sizeof(ExhGroup) * groups.size(), cudaMemcpyHostToDevice, x0);
         if (e == cudaSuccess && nitems > 0)
-            e = cudaMemcpyAsync(xitems_d, xitems.data(), sizeof(ExhItem) * nitems, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, st);
+            e = cudaMemcpyAsync(xitems_d, xitems.data(), sizeof(ExhItem) * nitems, cudaMemcpyHostToDevice, x0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(full_list, fl.data(), sizeof(int) * nfull, cudaMemcpyHostToDevice, x0);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(item_begin_d, ibeg.data(), sizeof(int) * (nfull + 1), cudaMemcpyHostToDevice, x0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(x0);  // the host vectors may go
         R.nfull = nfull;
         const size_t tsmem = tile_smem_bytes(m);
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(rescore_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
+        auto tile_fn = m == 512 ? rescore_tile_kernel<16> : m == 256 ? rescore_tile_kernel<8> : rescore_tile_kernel<0>;
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(tile_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(merge_chunks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        if (e == cudaSuccess && koff[2] > koff[1])
+            e = cudaFuncSetAttribute(filter_tile_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem8);
+        if (e == cudaSuccess && koff[3] > koff[2])
+            e = cudaFuncSetAttribute(filter_tile_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem4);
         if (e == cudaSuccess && nitems > 0) {
-            rescore_tile_kernel<<<(unsigned)nitems, 256, tsmem, st>>>(R, groups_d, xitems_d, item_begin_d, cand_chunk, tpc,
-                                                                       units_d, S->lvl_id, S->b_id_ds, partial);
-            merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, st>>>(R, item_begin_d, partial);
+            // the kinds run side by side; merge_chunks waits for all three
+            if (koff[1] > koff[0]) {
+                tile_fn<<<(unsigned)(koff[1] - koff[0]), 256, tsmem, x0>>>(
+                    R, groups_d, xitems_d + koff[0], item_begin_d, kchunk[0], ktpc[0], units_d, S->lvl_id, S->b_id_ds,
+                    partial);
+                ++launches;
+            }
+            if (koff[2] > koff[1]) {
+                filter_tile_kernel<8><<<(unsigned)(koff[2] - koff[1]), 256, fsmem8, aux[1]>>>(
+                    R, groups_d, xitems_d + koff[1], item_begin_d, kchunk[1], ktpc[1], units_d, S->lvl_id, S->b_id_ds,
+                    partial);
+                ++launches;
+            }
+            if (koff[3] > koff[2]) {
+                filter_tile_kernel<4><<<(unsigned)(koff[3] - koff[2]), 256, fsmem4, aux[2]>>>(
+                    R, groups_d, xitems_d + koff[2], item_begin_d, kchunk[2], ktpc[2], units_d, S->lvl_id, S->b_id_ds,
+                    partial);
+                ++launches;
+            }
+            if (koff[4] > koff[3]) {
+                const int nw = koff[4] - koff[3];
+                rescore_warp_kernel<<<(unsigned)((nw + 7) / 8), 256, 0, aux[3]>>>(
+                    R, groups_d, xitems_d + koff[3], nw, item_begin_d, kchunk[3], ktpc[3], units_d, S->lvl_id,
+                    S->b_id_ds, partial);
+                ++launches;
+            }
             e = cudaGetLastError();
-            launches += 2;
+            for (int a = 1; a < 4; ++a) {
+                if (e == cudaSuccess) e = cudaEventRecord(ev_aux[a], aux[a]);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(x0, ev_aux[a], 0);
+            }
+            if (e == cudaSuccess) {
+                merge_chunks_kernel<<<(unsigned)((nfull + rwpb - 1) / rwpb), 32 * rwpb, rsmem, x0>>>(R, item_begin_d, partial);
+                e = cudaGetLastError();
+                ++launches;
+            }
         }
-        // (host vectors stay alive until the synchronisation below)
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev_aux[4], x0);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev_aux[4], 0);
+        if (e != cudaSuccess)  // nothing of the side streams may outlive the buffers freed below
+            for (auto& a : aux)
+                if (a) cudaStreamSynchronize(a);
     }
+    for (auto& a : aux)
+        if (a) cudaStreamDestroy(a);
+    for (auto& v : ev_aux)
+        if (v) cudaEventDestroy(v);
+    if (ev_ovf) cudaEventDestroy(ev_ovf);
     if (e == cudaSuccess && parts > 1) {
         merge_parts_kernel<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(part_idx, part_dist, nq, parts, k,
                                                                      (long long*)out_idx, out_dist);

@@ -101,3 +101,28 @@ def test_new_points_scattered_with_tiny_p(cuda_available):
     for sub in (np.arange(5), np.array([3, 41, 44, 47])):
         ai, ad = index.knn_points_device(qv[sub], qp[sub], Xq[sub], k, form="screened")
         assert np.array_equal(ai.cpu().numpy(), si[sub]) and np.array_equal(ad.cpu().numpy(), sd[sub])
+
+
+def test_new_points_forced_exhaustive_pass(cuda_available, monkeypatch):
+    """Smooth tree (Matern l=2) and a survivor cap of 32 per column half: most new
+    points' slots overflow into the exhaustive pass and its certified FP32 filter;
+    against FP64, bit-identical to the rows of the survivor pass, and each row
+    against FP64 alone and in the mix."""
+    from covertreex_gb300.device import CudaResidualIndex
+
+    n, d, m, kt, ls, k, nq = 16384, 3, 128, 1, 2.0, 40, 600
+    X, V, p, Xq, qv, qp = _case(n, d, m, kt, ls, nq, seed=77)
+    lsv = np.full(d, ls, np.float32)
+    index = CudaResidualIndex(V, p, X, variance=1.0, lengthscale=ls, kernel_type=kt, build_tree=False)
+    ri, rd = index.knn_points_device(qv, qp, Xq, k, form="screened")
+    monkeypatch.setenv("CT_SCREEN_SURVIVOR_CAP", "64")
+    si, sd = index.knn_points_device(qv, qp, Xq, k, form="screened")
+    assert index.last_stats["overflow_queries"] > 100
+    si, sd = si.cpu().numpy(), sd.cpu().numpy()
+    _check_screened_vs_fp64(V, p, X, Xq, qv, qp, si, sd, kt, lsv, k)
+    # the same rows as through the survivor pass, bit for bit
+    assert np.array_equal(ri.cpu().numpy(), si) and np.array_equal(rd.cpu().numpy().view(np.uint32), sd.view(np.uint32))
+    for sub in (np.arange(9), np.arange(2, nq, 11)):
+        ai, ad = index.knn_points_device(qv[sub], qp[sub], Xq[sub], k, form="screened")
+        ai, ad = ai.cpu().numpy(), ad.cpu().numpy()
+        _check_screened_vs_fp64(V, p, X, Xq[sub], qv[sub], qp[sub], ai, ad, kt, lsv, k)

@@ -129,3 +129,26 @@ def test_screened_matches_dense_where_well_conditioned(cuda_available):
     good = case["p"] >= 0.05
     agree = np.mean([set(a) == set(b) for a, b, g in zip(di, si, good) if g])
     assert agree > 0.99
+
+
+@pytest.mark.parametrize("predecessor", [False, True])
+def test_screened_forced_exhaustive_pass_vs_fp64(cuda_available, monkeypatch, predecessor):
+    """A survivor cap of 32 per column half overflows most query slots of a smooth
+    Matern l=2 case, so the exhaustive pass runs over well-conditioned queries: its
+    certified FP32 filter (exact distances only where the lower bound reaches the
+    query's threshold) must leave the answer equal to FP64.  Every pass computes a pair's
+    exact distance from the same double-float dot, so the rows equal those of the
+    survivor pass bit for bit."""
+    case = gaussian_case(12000, 3, 128, 1, 2.0, seed=21)
+    idx = _index(case)
+    q = np.random.default_rng(22).choice(12000, 500, replace=False).astype(np.int64)
+    monkeypatch.setenv("CT_SCREEN_SURVIVOR_CAP", "64")
+    gi, gd = idx.knn(q, 40, predecessor=predecessor, form="screened")
+    st = idx.last_stats
+    assert st["overflow_queries"] > 100
+    _check_against_fp64(case, q, 40, predecessor, gi, gd)
+    # the same queries through the survivor pass
+    monkeypatch.delenv("CT_SCREEN_SURVIVOR_CAP")
+    hi, hd = idx.knn(q, 40, predecessor=predecessor, form="screened")
+    assert idx.last_stats["overflow_queries"] < st["overflow_queries"]
+    assert np.array_equal(hi, gi) and np.array_equal(hd.view(np.uint32), gd.view(np.uint32))

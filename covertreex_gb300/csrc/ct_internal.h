@@ -38,6 +38,7 @@ cudaError_t compute_order(const float* coords, long long n, int d, int mode, int
                           unsigned long long* keys_by_id = nullptr, double* bounds_out = nullptr);
 cudaError_t hilbert_keys_bounded(const float* coords, long long n, int d, const double* bounds,
                                  unsigned long long* keys, int* scratch_vals, cudaStream_t st);
+int radix_sort_launches(long long n, int kbits);
 cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long long* ktmp, int* vtmp, long long n,
                              int kbits, unsigned* hist, void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st,
                              bool* result_in_tmp);

@@ -6,7 +6,8 @@
 // `bits = clamp(64 / D, 1, 16)` bits with round-half-even, Skilling's
 // axes-to-transpose, bit interleave.  Order = stable sort by (key, index).
 //
-// The sort is a least-significant-digit radix sort over 8-bit digits: per pass
+// Up to 4096 pairs sort in one block (bitonic, by key then position).  Larger sets
+// take a least-significant-digit radix sort over 8-bit digits: per pass
 // a per-block histogram, one exclusive scan over (digit, block), and a stable
 // scatter in which each block ranks its keys with warp ballots.  No
 // inter-block waiting, so nothing can spin.
@@ -220,12 +221,58 @@ __global__ void __launch_bounds__(1024) scan_exclusive_kernel(unsigned* __restri
     }
 }
 
+// Up to kSmallSort pairs: one block, a bitonic sort in shared memory by (key, val).
+// The values are the input positions (ascending), so this is the stable order by key
+// that the radix passes give, in one launch instead of three per digit.
+constexpr int kSmallSort = 4096;
+__global__ void __launch_bounds__(1024) small_sort_pairs_kernel(unsigned long long* __restrict__ keys,
+                                                                int* __restrict__ vals, int n) {
+    __shared__ unsigned long long sk[kSmallSort];
+    __shared__ int sv[kSmallSort];
+    int np = 2;
+    while (np < n) np <<= 1;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        sk[i] = i < n ? keys[i] : ~0ULL;
+        sv[i] = i < n ? vals[i] : 0x7fffffff;
+    }
+    __syncthreads();
+    for (int size = 2; size <= np; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < np / 2; i += blockDim.x) {
+                const int lo = 2 * i - (i & (stride - 1));
+                const int hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const unsigned long long ka = sk[lo], kb = sk[hi];
+                const int va = sv[lo], vb = sv[hi];
+                const bool gt = ka > kb || (ka == kb && va > vb);
+                if (gt == up) {
+                    sk[lo] = kb; sk[hi] = ka;
+                    sv[lo] = vb; sv[hi] = va;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        keys[i] = sk[i];
+        vals[i] = sv[i];
+    }
+}
+
 }  // namespace
 
-// Sort (keys, vals) ascending by key, stable.  `kbits` = number of key bits used.
+int radix_sort_launches(long long n, int kbits) { return n <= kSmallSort ? 1 : 3 * ((kbits + 7) / 8); }
+
+// Sort (keys, vals) ascending by key, stable (vals must be the input positions when n
+// is at most kSmallSort).  `kbits` = number of key bits used.
 cudaError_t radix_sort_pairs(unsigned long long* keys, int* vals, unsigned long long* ktmp, int* vtmp, long long n,
                              int kbits, unsigned* hist, void* scan_tmp, size_t scan_tmp_bytes, cudaStream_t st,
                              bool* result_in_tmp) {
+    if (n <= kSmallSort) {
+        if (n > 1) small_sort_pairs_kernel<<<1, 1024, 0, st>>>(keys, vals, (int)n);
+        *result_in_tmp = false;
+        return cudaGetLastError();
+    }
     const int nblocks = (int)((n + kTile - 1) / kTile);
     unsigned long long *ka = keys, *kb = ktmp;
     int *va = vals, *vb = vtmp;

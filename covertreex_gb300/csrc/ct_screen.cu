@@ -119,6 +119,7 @@ struct MMAParams {
     int nstages;
     float* out_f;        // debug output
     int* surv; int* surv_cnt;
+    float* survb;        // per survivor: the upper bound of |rho| / sqrt(p_q) that kept it
     int half_cap;        // survivor segment per (slot, column half)
     const float* rec[2]; // candidate records in tile order (levels, dataset), RT floats per tile
     const unsigned* xmax_max;  // bits of max |x_c| over the dataset rows
@@ -400,7 +401,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
             const int acc = lt & 1;
             const unsigned aph = (unsigned)((lt >> 1) & 1);
             if (MODE == MODE_SWEEP && jb.first) {
-                if (slot >= 0) P.surv_cnt[2 * slot + half] = cnt;
+                if (slot >= 0) {
+                    P.surv_cnt[2 * slot + half] = cnt;
+                    // the final threshold, for the survivor pass (parts > 1 share it during the sweep)
+                    if (P.parts == 1 && qid >= 0) atomicMin(&P.qtau[slot], __float_as_uint(tau2));
+                }
                 const long long arow = (long long)jb.qtile * TQ + row;
                 slot = P.a_slot[arow];
                 qid = slot >= 0 ? P.slot_id[slot] : -1;
@@ -581,7 +586,10 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     if (keep_job && bhi[i] >= thr_keep) {
-                        if (cnt < P.half_cap) P.surv[((size_t)slot * 2 + half) * P.half_cap + cnt] = bid[i];
+                        if (cnt < P.half_cap) {
+                            P.surv[((size_t)slot * 2 + half) * P.half_cap + cnt] = bid[i];
+                            P.survb[((size_t)slot * 2 + half) * P.half_cap + cnt] = bhi[i];
+                        }
                         if (++cnt > P.half_cap) {
                             ovf = true;
                             thr_keep = __int_as_float(0x7f800000);
@@ -624,7 +632,11 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
         __syncwarp();
         if (lane == 0) release_unit(ui);
         }
-        if (MODE == MODE_SWEEP && slot >= 0) P.surv_cnt[2 * slot + half] = cnt;
+        if (MODE == MODE_SWEEP && slot >= 0) {
+            P.surv_cnt[2 * slot + half] = cnt;
+            // the final threshold, for the survivor pass (parts > 1 share it during the sweep)
+            if (P.parts == 1 && qid >= 0) atomicMin(&P.qtau[slot], __float_as_uint(tau2));
+        }
     }
     sm::tc_fence_before();
     __syncthreads();
@@ -786,6 +798,7 @@ struct RescoreParams {
     long long n;
     const int* slot_id; long long nslots;
     const int* surv; const int* surv_cnt; int half_cap;
+    const float* survb;  // the sweep's bound of each survivor (see MMAParams)
     const int* full_slots; int nfull;  // slots rescored against every valid candidate
     int k;
     long long* out_idx; float* out_dist;
@@ -1119,7 +1132,6 @@ __global__ void rescore_kernel(RescoreParams P) {
         return;
     }
     const int k = P.k;
-    const int count = c0 + c1;  // <= 2 half_cap <= RBUF
     float vql[32];
     load_query_slice(P.v + (size_t)q * P.m, P.m, vql);
     // per-query constants of the bounds
@@ -1129,12 +1141,32 @@ __global__ void rescore_kernel(RescoreParams P) {
     const float A = 2.4e-7f * (P.xmax[q] + __uint_as_float(__ldg(P.xmax_max)));
     const float ale = (ced2 + 0.5f * A * dd) * 1.00001f, bee = 0.5f * A * 1.00001f;
     const float alk = (6e-8f + 0.5f * ced2 + 0.25f * A * dd) * 1.00001f, bek = (1e-6f + 0.25f * A) * 1.00001f;
-    // ---- F: certified FP32 bounds of every survivor
+    // ---- survivors the query's final threshold excludes (the sweep's own keep test with
+    // the threshold it ended with: any part's k-th upper bound) are dropped before any row
+    // is read; the others are compacted into keys (ids in the low bits)
+    int count = 0;
+    const float tq = __uint_as_float(__ldcg(&P.qtau[slot / P.parts]));
+    {
+        const float thr = (1.f - tq) * (1.f - 2e-6f) / isq;
+        for (int base = 0; base < c0 + c1; base += 32) {
+            const int ci = base + lane;
+            int cid = -1;
+            bool keep = false;
+            if (ci < c0 + c1) {
+                const size_t o = ci < c0 ? (size_t)(2 * slot) * P.half_cap + ci : (size_t)(2 * slot + 1) * P.half_cap + (ci - c0);
+                cid = P.surv[o];
+                keep = P.survb[o] >= thr;
+            }
+            const unsigned mk = __ballot_sync(0xffffffffu, keep);
+            if (keep) keys[count + __popc(mk & ((1u << lane) - 1u))] = (unsigned long long)(unsigned)cid;
+            count += __popc(mk);
+        }
+        __syncwarp();
+    }
+    // ---- F: certified FP32 bounds of every remaining survivor
     for (int base = 0; base < count; base += 32) {
         const int ci = base + lane;
-        const int cid = ci < count ? (ci < c0 ? P.surv[(size_t)(2 * slot) * P.half_cap + ci]
-                                              : P.surv[(size_t)(2 * slot + 1) * P.half_cap + (ci - c0)])
-                                   : -1;
+        const int cid = ci < count ? (int)(unsigned)(keys[ci] & 0xffffffffULL) : -1;
         const int nb = count - base < 32 ? count - base : 32;
         float mydot = 0.f;
         for (int t = 0; t < nb; t += 4) {
@@ -1174,6 +1206,9 @@ __global__ void rescore_kernel(RescoreParams P) {
         const float margin = 4e-12f * fminf(isq * __uint_as_float(__ldg(P.isp_max)) * 1.01f, 1e9f) + 1e-12f;
         tau = __fadd_ru(__fmul_ru(__uint_as_float(lo), 1.000004f), margin);
     }
+    // the query's final threshold bounds its k-th distance over all parts: a part slot
+    // rescores only what can enter the query's top k, not its own k best
+    tau = fminf(tau, tq);
     __syncwarp();
     // compaction of the survivors that can still be among the k nearest
     int nk = 0;
@@ -1252,10 +1287,17 @@ __global__ void merge_chunks_kernel(RescoreParams P, const int* item_begin, cons
     __syncwarp();
     int fill = k;
     const long long e0 = (long long)item_begin[w] * k, e1 = (long long)item_begin[w + 1] * k;
-    for (long long base = e0; base < e1; base += 32) {
-        const bool has = base + lane < e1;
-        const unsigned long long key = has ? partial[base + lane] : ~0ULL;
-        warp_topk_append(keys, fill, k, has && key != ~0ULL, key);
+    // 128 keys per round, loads issued together; chunk lists are mostly padding
+    for (long long base = e0; base < e1; base += 128) {
+        unsigned long long key[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long long o = base + 32 * u + lane;
+            key[u] = o < e1 ? __ldcs(partial + o) : ~0ULL;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (__any_sync(0xffffffffu, key[u] != ~0ULL)) warp_topk_append(keys, fill, k, key[u] != ~0ULL, key[u]);
     }
     warp_bitonic_sort(keys, sort_len(fill));
     for (int j = lane; j < k; j += 32) {
@@ -2324,6 +2366,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     int *a_slot_lvl = nullptr, *rowmap_lvl = nullptr;
     int *a_slot_x = nullptr, *rowmap_x = nullptr, *slot_id_x = nullptr;  // part-expanded (parts > 1)
     bf16 *al_hi = nullptr, *al_lo = nullptr;
+    float* survb = nullptr;
     int *surv = nullptr, *surv_cnt = nullptr, *full_list = nullptr, *nfull_d = nullptr, *unit_counter = nullptr;
     int2* unit_jobs_d = nullptr;
     long long* part_idx = nullptr;
@@ -2353,7 +2396,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     ++launches;
     bool in_tmp = false;
     const int kb_lvl = 64;
-    launches += 3 * ((kb_lvl + 7) / 8) + 2;
+    launches += ct::radix_sort_launches(nq, kb_lvl) + 2;
     e = ct::radix_sort_pairs(key_lvl, val_lvl, ktmp, vtmp, nq, kb_lvl, hist, nullptr, 0, st, &in_tmp);
     if (e == cudaSuccess && in_tmp) { e = cudaMemcpyAsync(val_lvl, vtmp, sizeof(int) * nq, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(key_lvl, ktmp, 8 * nq, cudaMemcpyDeviceToDevice, st); }
@@ -2519,6 +2562,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     }
     A((void**)&al_hi, sizeof(bf16) * rows_x * m); A((void**)&al_lo, sizeof(bf16) * rows_x * m);
     A((void**)&surv, sizeof(int) * nslots * 2 * (size_t)half_cap);
+    A((void**)&survb, sizeof(float) * nslots * 2 * (size_t)half_cap);
     A((void**)&surv_cnt, sizeof(int) * 2 * nslots);
     A((void**)&full_list, sizeof(int) * nslots);
     A((void**)&jobs, sizeof(Job) * (njobs + 1));
@@ -2556,7 +2600,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     P.xs = xs; P.d = d; P.vn = S->vn; P.isp = S->isp; P.xmax = S->xmax;
     P.var = var; P.kernel_type = kernel_type; P.predecessor = predecessor ? 1 : 0;
     P.err_coef = err_coef_for(m); P.k = k; P.nstages = nstages;
-    P.surv = surv; P.surv_cnt = surv_cnt; P.half_cap = half_cap; P.status = S->status;
+    P.surv = surv; P.surv_cnt = surv_cnt; P.half_cap = half_cap; P.status = S->status; P.survb = survb;
     P.qtau = qtau; P.parts = parts;
     P.rec[0] = S->rec_lvl; P.rec[1] = S->rec_ds; P.xmax_max = S->xmax_max;
     if (e == cudaSuccess) { e = launch_sweep(P, MODE_SWEEP, ncta, st); ++launches; }
@@ -2566,6 +2610,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     R.v = vnat; R.m = m; R.coords = coords_raw; R.d = d; R.inv_ls_df = S->inv_ls_df; R.p = p;
     R.var = var; R.kernel_type = kernel_type; R.predecessor = predecessor ? 1 : 0; R.n = n;
     R.slot_id = slot_id_use; R.nslots = nslots; R.surv = surv; R.surv_cnt = surv_cnt; R.half_cap = half_cap;
+    R.survb = survb;
     R.full_slots = full_list;
     R.nfull = 0; R.chunk = 4096;
     R.k = k; R.evals = evals_d;
@@ -2830,7 +2875,7 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
     cudaFreeAsync(key_lvl, st); cudaFreeAsync(ktmp, st); cudaFreeAsync(hist, st);
     cudaFreeAsync(a_slot_lvl, st); cudaFreeAsync(rowmap_lvl, st);
     cudaFreeAsync(al_hi, st); cudaFreeAsync(al_lo, st);
-    cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st);
+    cudaFreeAsync(surv, st); cudaFreeAsync(surv_cnt, st); cudaFreeAsync(survb, st);
     cudaFreeAsync(full_list, st); cudaFreeAsync(nfull_d, st); cudaFreeAsync(evals_d, st);
     cudaFreeAsync(jobs, st); cudaFreeAsync(unit_jobs_d, st); cudaFreeAsync(unit_counter, st); cudaFreeAsync(qtau, st);
     if (units_d) cudaFreeAsync(units_d, st);

@@ -166,22 +166,24 @@ __global__ void kxm_kernel(const double* __restrict__ x, long long r0, long long
     Kc[e] = kernel_f64(x + (size_t)(r0 + r) * d, z + (size_t)t * d, d, kt, var, ls);
 }
 
-// Vc[r][j] = sum_{t <= j} Kc[r][t] Li[j][t]; 64 x 64 tile, 256 threads, 4 x 4 each.
-constexpr int GT = 64;
-constexpr int GK = 16;
+// Vc[r][j] = sum_{t <= j} Kc[r][t] Li[j][t]; 32 x 32 tile, 256 threads, 2 x 2 each.  The
+// small tile keeps each block short (GB300's FP64 rate is low): a serving build's blocks
+// then free their SMs quickly for the query kernels on higher-priority streams.
+constexpr int GT = 32;
+constexpr int GK = 32;
 __global__ void __launch_bounds__(256) dgemm_lt_kernel(const double* __restrict__ Kc, long long rows,
                                                        const double* __restrict__ Li, int m,
                                                        double* __restrict__ Vc) {
-    __shared__ double As[GK][GT];
-    __shared__ double Bs[GK][GT];
+    __shared__ double As[GK][GT + 1];
+    __shared__ double Bs[GK][GT + 1];
     const long long r0 = (long long)blockIdx.y * GT;
     const int j0 = blockIdx.x * GT;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    double acc[4][4];
+    double acc[2][2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
+    for (int u = 0; u < 2; ++u)
 #pragma unroll
-        for (int w = 0; w < 4; ++w) acc[u][w] = 0.0;
+        for (int w = 0; w < 2; ++w) acc[u][w] = 0.0;
     const int kend = min(m, j0 + GT);  // Li[j][t] = 0 for t > j
     for (int t0 = 0; t0 < kend; t0 += GK) {
         for (int e = threadIdx.x; e < GT * GK; e += 256) {
@@ -193,27 +195,27 @@ __global__ void __launch_bounds__(256) dgemm_lt_kernel(const double* __restrict_
             Bs[tt][rr] = (j < m && t < m) ? Li[(size_t)j * m + t] : 0.0;
         }
         __syncthreads();
-#pragma unroll
+#pragma unroll 8
         for (int tt = 0; tt < GK; ++tt) {
-            double a[4], b[4];
+            double a[2], b[2];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < 2; ++u) {
                 a[u] = As[tt][ty + 16 * u];
                 b[u] = Bs[tt][tx + 16 * u];
             }
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 2; ++u)
 #pragma unroll
-                for (int w = 0; w < 4; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
+                for (int w = 0; w < 2; ++w) acc[u][w] = fma(a[u], b[w], acc[u][w]);
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
         const long long row = r0 + ty + 16 * u;
         if (row >= rows) continue;
 #pragma unroll
-        for (int w = 0; w < 4; ++w) {
+        for (int w = 0; w < 2; ++w) {
             const int j = j0 + tx + 16 * w;
             if (j < m) Vc[row * m + j] = acc[u][w];
         }

@@ -1,7 +1,9 @@
 """Soundness of the certified bounds of the precision form, checked on the CPU: the FP32
 filter of the survivor pass (ct_screen.cu: warp_dots_f32 + pair_bounds_f32 and the
-per-query constants of two_level_topk) and the sweep epilogue's bounds on |rho| for any
-tensor-core dot within the certified BF16 error band (screen_sweep_kernel, phase 1).
+per-query constants of two_level_topk), the FP32 GEMM filter of the exhaustive pass
+(filter_tile_kernel: blocked sums of FMA chains of 16 elements, pair_bounds_core) and the
+sweep epilogue's bounds on |rho| for any tensor-core dot within the certified BF16 error
+band (screen_sweep_kernel, phase 1).
 
 The kernel's float32 arithmetic is restated operation by operation in numpy: each of the
 32 lanes runs an FMA chain over its m/32 contiguous elements, a butterfly of additions
@@ -49,11 +51,27 @@ def dot_f32(vq, vc, m):
     return s[0]
 
 
-def bounds(q, c, data, exp_pick):
-    """[dl2, du2] of the pair as the kernel computes them (exp_pick: 0 nominal, 1 low, 2 high)."""
+def dot_blocked(vq, vc, m, flb=16):
+    """filter_tile_kernel's dot: FMA chains of flb consecutive elements, each added to a total."""
+    tot = F(0.0)
+    for b in range(0, m, flb):
+        acc = F(0.0)
+        for e in range(b, b + flb):
+            acc = fma32(vq[e], vc[e], acc)
+        tot = F(tot + acc)
+    return tot
+
+
+def bounds(q, c, data, exp_pick, kind="survivor"):
+    """[dl2, du2] of the pair as the kernel computes them (exp_pick: 0 nominal, 1 low, 2 high;
+    kind: the survivor pass's lane chains or the exhaustive pass's blocked GEMM sums)."""
     Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
-    dot = dot_f32(Vf[q], Vf[c], m)
-    ed_q = F(F(F((m >> 5) + 7) * F(5.97e-8)) * vn[q])
+    if kind == "survivor":
+        dot = dot_f32(Vf[q], Vf[c], m)
+        ed_q = F(F(F((m >> 5) + 7) * F(5.97e-8)) * vn[q])
+    else:
+        dot = dot_blocked(Vf[q], Vf[c], m)
+        ed_q = F(F(F(16 + m // 16 + 1) * F(5.97e-8)) * vn[q])
     ed = F(ed_q * vn[c])
     dd = F(d)
     ced2 = F(F(dd + F(2.0)) * F(5.97e-8))
@@ -106,13 +124,14 @@ def _case(n, d, m, kt, ls, seed, dup=8):
     return X, V, p, idx, data
 
 
+@pytest.mark.parametrize("kind", ["survivor", "gemm"])
 @pytest.mark.parametrize("n,d,m,kt,ls", [
     (1500, 3, 64, 1, 1.0),   # Matern 5/2, serving-like
     (1500, 8, 64, 0, 2.0),   # RBF, precision-workload-like
     (1200, 3, 128, 0, 0.7),  # RBF, short lengthscale, m % 128 == 0 (float4 lane shares)
     (1200, 5, 96, 1, 2.0),   # Matern, m % 128 != 0 (scalar lane shares)
 ])
-def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls):
+def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls, kind):
     X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m)
     r = np.random.default_rng(7)
     pairs = [tuple(r.choice(n, 2, replace=False)) for _ in range(120)]
@@ -128,7 +147,7 @@ def test_fp32_filter_bounds_contain_fp64(n, d, m, kt, ls):
             continue
         truth = float(O.residual_dist_f64(V, p, X, 1.0, ls_vec, kt, [q], [c])[0, 0]) ** 2
         for pick in (0, 1, 2):
-            dl2, du2 = bounds(q, c, data, pick)
+            dl2, du2 = bounds(q, c, data, pick, kind)
             assert dl2 <= truth <= du2, (q, c, pick, dl2, truth, du2)
         if i < 120:
             widths.append(du2 - dl2)

@@ -57,6 +57,9 @@ def parse_args():
     ap.add_argument("--tree-queries", type=int, default=4096, help="sampled queries of the tree-form measurement")
     ap.add_argument("--serving-rates", default="100,500,1000", help="request rates (req/s) of the serving sweep")
     ap.add_argument("--serving-seconds", type=float, default=2.0, help="arrival window per serving rate")
+    ap.add_argument("--new-points-request", default=None, metavar="N,LS,Q",
+                    help="profiling aid: one screened request of Q new points against a serving-shaped tree of N "
+                         "points (D=3, Matern 5/2 lengthscale LS, m=256), timed alone; no bench line")
     return ap.parse_args()
 
 
@@ -488,6 +491,42 @@ def bench_serving(dev, rates, seconds: float):
             "p99_target_ms": 5.0}
 
 
+# ------------------------------------------------------------------ one serving-shaped request
+def bench_new_points_request(dev, n: int, ls: float, q: int, reps: int = 3):
+    """Profiling aid: a serving-shaped tree (N(0,1) coordinates in D=3, seed 7; Matern 5/2,
+    lengthscale ls, m=256 inducing points, seed 11; V and p by the GPU FP64 factor) and one
+    screened request of q new N(0,1) points (seed q), k=60, timed alone."""
+    import torch
+    from covertreex_gb300 import _lib
+    from covertreex_gb300.device import CudaResidualIndex, CudaVFactor
+    from covertreex_gb300.residual import inducing_indices
+
+    _lib.load().ct_set_timing(1)
+    X = np.random.default_rng(7).standard_normal((n, 3)).astype(np.float32)
+    ind = inducing_indices(n, 256, 11)
+    f = CudaVFactor(X[ind].astype(np.float64), kernel_type=1, variance=1.0, lengthscale=ls, device=dev)
+    V, p = f.embed_device(torch.as_tensor(X, device=dev))
+    idx = CudaResidualIndex(V, p, X, variance=1.0, lengthscale=[ls] * 3, kernel_type=1, build_tree=False,
+                            query_slab=True, device=dev)
+    idx.prepare_screened()
+    Q = torch.as_tensor(np.random.default_rng(q).standard_normal((q, 3)).astype(np.float32), device=dev)
+    qv, qp = f.embed_device(Q)
+    runs = []
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        idx.knn_points_device(qv, qp, Q, 60, form="screened")
+        torch.cuda.synchronize()
+        st = dict(idx.last_stats)
+        runs.append({"ms": (time.perf_counter() - t0) * 1e3,
+                     **{key: st[key] for key in ("threshold_ms", "screen_ms", "rescore_ms", "overflow_queries",
+                                                 "pairs_exhaustive", "pairs_rescored", "kernel_launches")}})
+    _lib.load().ct_set_timing(0)
+    idx.free()
+    f.free()
+    return {"request": {"n": n, "lengthscale": ls, "points": q, "k": 60, "m": 256, "d": 3}, "runs": runs}
+
+
 # ------------------------------------------------------------------ GPU leg
 def main():
     args = parse_args()
@@ -512,6 +551,12 @@ def main():
 
     _build.build_library()
     L = _lib.load()
+    if args.new_points_request:
+        if rank == 0:
+            n_s, ls_s, q_s = args.new_points_request.split(",")
+            print(json.dumps(bench_new_points_request(torch.device("cuda", local), int(n_s), float(ls_s), int(q_s),
+                                                      reps=max(1, args.steps))))
+        return
     if args.no_headline:
         # profiling aid: the batching / serving forms alone (not the bench line)
         dev = torch.device("cuda", local)
@@ -688,11 +733,11 @@ def main():
         try:
             subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], check=True)
             threads = os.cpu_count() or 1
-            qps, tree = oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False)
+            qps, otree = oracle_queries_per_s(wl, args.cpu_sample, threads, parity=False)
             cpu = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                    "sample": f"{min(args.cpu_sample, wl.n)} random query ids of the same workload, default budget "
-                             f"mode; tree build {tree.build_seconds:.2f} s excluded"}
-            del tree
+                             f"mode; tree build {otree.build_seconds:.2f} s excluded"}
+            del otree
             # the reference's parity mode (COVERTREEX_RESIDUAL_PARITY=1: no budget ladder,
             # exhaustive up to the cover-radius prune), reported separately
             pq = max(16, args.cpu_sample // 32)

@@ -683,14 +683,16 @@ def main():
     alg_flops = 2.0 * wl.m * alg_pairs
     issued_flops = 3.0 * 2.0 * wl.m * pairs_main    # hi.hi + hi.lo + lo.hi per screened pair
     achieved = alg_flops / (screen_ms / 1e3) / 1e12
-    # DRAM bytes per screened pair of the sweep, from an ncu capture of the same kernel on
-    # the N=65536 case of this workload, scaled to this launch
-    sweep_dram_bytes_per_pair = 7.19
+    # DRAM bytes per screened pair of the sweep, from a one-pass ncu capture of a full-size
+    # launch of this workload, scaled to this launch's pairs
+    sweep_dram_bytes_per_pair = 11.39
     roofline = {
         "bound": "tensor", "kernel": "screen_sweep_kernel (main sweep)", "achieved": achieved,
         "peak": bf16_sus, "unit": "TFLOP/s", "frac": achieved / bf16_sus,
         "traffic": sweep_dram_bytes_per_pair * pairs_main,
-        "traffic_note": "bytes per launch: 7.19 B per screened pair (ncu, N=65536) x pairs of this launch",
+        "traffic_note": "bytes per launch: 11.39 B per screened pair x pairs of this launch (ncu "
+                        "dram__bytes_read.sum + dram__bytes_write.sum of one full-size sweep launch, one pass: "
+                        "423.4 GB for 3.718e10 pairs)",
         "peak_kind": f"bf16_tflops_sustained ({peak_kind})",
         "tensor_issued_tflops": issued_flops / (screen_ms / 1e3) / 1e12,
         "kernel_ms": screen_ms, "algorithmic_pairs": alg_pairs, "pairs_screened": pairs_main,

@@ -10,15 +10,17 @@
 //   2. Sweep.  A CTA owns a tile of 128 queries (sorted by Hilbert position
 //      inside their "level": the dataset prefix [0, 2^j) with 2^j <= q in
 //      predecessor mode, the whole dataset otherwise) and sweeps its candidate
-//      tiles nearest-first: the level's Hilbert tiles in a spiral around the
-//      queries, then (predecessor mode) the dataset tiles [2^j, max q).  For every
+//      tiles: a warm-up over the level's Hilbert tiles nearest-first (a spiral
+//      around the queries), then the level's tiles (ascending in one-part calls,
+//      the spiral in split calls) and (predecessor mode) the dataset tiles
+//      [2^j, max q).  For every
 //      query x candidate pair, s = hi.hi + hi.lo + lo.hi is accumulated in TMEM
 //      by tcgen05.mma (kind::f16, M=128, N=256, K=16) and the epilogue turns it
 //      into certified bounds [dl2, du2] of the squared residual distance.  Each
 //      epilogue thread keeps the k smallest du2 of its row half in a heap; the
 //      k-th is an upper bound tau^2 of the true k-th distance, and every
 //      candidate with dl2 <= tau^2 (tau as it stands when the pair is seen) is
-//      kept.  Spiral order makes tau tight after the first tiles.
+//      kept.  The nearest-first warm-up makes tau tight before any pair is kept.
 //   3. Rescore.  Each survivor's distance is recomputed from the f32 inputs with
 //      a compensated FP32 dot product (TwoProd/TwoSum) and an FP64 kernel value
 //      and normalisation; the k best (distance, index) pairs are written out.
@@ -1069,13 +1071,14 @@ __device__ __forceinline__ void warp_dots_f32(const float* __restrict__ V, int m
 // Certified bounds [dl2, du2] of d^2 = 1 - |rho| for one pair from an FP32 dot with
 // error <= ed: the kernel value from the scaled f32 coordinates with the sweep's error
 // model (ale, bee, alk, bek as there), the normalisation 1 / sqrt(max(p_q p_c, 1e-18)).
-// xq, xc: the pair's scaled coordinates (global or shared memory); isc = 1 / sqrt(p_c).
+// xq, xc: the pair's scaled coordinates (global or shared memory; the candidate's axes
+// xc_stride apart); isc = 1 / sqrt(p_c).
 __device__ __forceinline__ void pair_bounds_core(const RescoreParams& P, const float* xq, const float* xc, float isc,
                                                  float dot, float ed, float isq, float alk, float bek, float ale,
-                                                 float bee, float& dl2, float& du2) {
+                                                 float bee, float& dl2, float& du2, int xc_stride = 1) {
     float d2 = 0.f;
     for (int a = 0; a < P.d; ++a) {
-        const float t = __fsub_rn(xc[a], xq[a]);
+        const float t = __fsub_rn(xc[a * xc_stride], xq[a]);
         d2 = __fmaf_rn(t, t, d2);
     }
     float kv, ek;
@@ -1397,6 +1400,7 @@ struct JobUnit {
     // predecessor or self test (flag 8): level tiles when the level size is at most
     // the tile's smallest query id, dataset tiles below ds_fast_end.
     int fast_lvl, ds_fast_end;
+    int lin;              // main sweep over the level tiles in ascending order (else the spiral)
 };
 
 // w-th tile of the spiral cc, cc+1, cc-1, cc+2, cc-2, ... clipped to [t0, t0 + ntl)
@@ -1407,6 +1411,20 @@ __device__ __forceinline__ int spiral_tile(const JobUnit& U, int w) {
     if (w <= 2 * mm) return (w & 1) ? U.cc + (w + 1) / 2 : U.cc - w / 2;
     return right > left ? U.cc + (w - mm) : U.cc - (w - mm);
 }
+// position of level tile t in that spiral (the inverse of spiral_tile)
+__device__ __forceinline__ int spiral_index(const JobUnit& U, int t) {
+    const int dd = t - U.cc;
+    if (dd == 0) return 0;
+    const int left = U.cc - U.t0, right = U.t0 + U.ntl - 1 - U.cc;
+    const int mm = left < right ? left : right;
+    const int ad = dd < 0 ? -dd : dd;
+    if (ad <= mm) return dd > 0 ? 2 * dd - 1 : 2 * ad;
+    return ad + mm;
+}
+// w-th level tile of the main sweep (w < ntl): ascending from t0, so that the units of a
+// level in flight on different SMs read the same candidate tiles at about the same time
+// and share them in L2; the warm-up has already taken the nearest tiles in spiral order.
+__device__ __forceinline__ int main_tile(const JobUnit& U, int w) { return U.lin ? U.t0 + w : spiral_tile(U, w); }
 
 // Exhaustive rescoring, tiled: a CTA takes a group of up to XQ overflowed query slots
 // that share a candidate source (the main pass: the id range [0, cend); the part pass:
@@ -1509,7 +1527,7 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
                 } else {
                     const int j = t_lo + (int)(o / TC);
                     const int wt = U.p + j * U.parts;
-                    const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                    const int* ids = wt < U.ntl ? lvl_id + (size_t)main_tile(U, wt) * TC
                                                 : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
                     cid = ids[o % TC];
                 }
@@ -1647,7 +1665,7 @@ __global__ void __launch_bounds__(256) rescore_warp_kernel(RescoreParams P, cons
                     cid = (int)(c_lo + o);
                 } else {
                     const int wt = U.p + (t_lo + (int)(o / TC)) * U.parts;
-                    const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                    const int* ids = wt < U.ntl ? lvl_id + (size_t)main_tile(U, wt) * TC
                                                 : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
                     cid = ids[o % TC];
                 }
@@ -1733,7 +1751,7 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
     float* qsT = cbuf + 2 * FCB * FKP;                                             // [m][FQP]
     unsigned long long* kb = (unsigned long long*)(qsT + (size_t)m * FQP);        // [FQ][XKB]
     unsigned char* plist = (unsigned char*)(kb + FQ * XKB);                       // [FQ][FCB]
-    float* cx = (float*)(plist + FQ * FCB);                                        // [FCB][8]
+    float* cx = (float*)(plist + FQ * FCB);                                        // [8][FCB] (axis-major)
     float* cisp = cx + FCB * 8;
     float* cvn = cisp + FCB;
     float* qc = cvn + FCB;        // [FQ][8]: isq, ed / |v_c|, alk, bek, ale, bee, margin, tau^2
@@ -1803,13 +1821,13 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
                 if (o < total) cid = (int)(c_lo + o);
             } else {
                 const int wt = U.p + (t_lo + b) * U.parts;
-                const int* ids = wt < U.ntl ? lvl_id + (size_t)spiral_tile(U, wt) * TC
+                const int* ids = wt < U.ntl ? lvl_id + (size_t)main_tile(U, wt) * TC
                                             : ds_id + (size_t)(U.lo_tile + (wt - U.ntl)) * TC;
                 cid = ids[tid];
             }
             cid_s[tid] = cid;
             if (cid >= 0) {
-                for (int a = 0; a < d; ++a) cx[tid * 8 + a] = P.xs[(size_t)cid * d + a];
+                for (int a = 0; a < d; ++a) cx[a * FCB + tid] = P.xs[(size_t)cid * d + a];
                 cisp[tid] = P.isp[cid];
                 cvn[tid] = P.vn[cid];
             }
@@ -1898,8 +1916,8 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
                 bool keep = cid >= 0 && !(P.predecessor && cid >= q);
                 if (keep && cid != q) {  // the query itself: d = 0
                     float dl2, du2;
-                    pair_bounds_core(P, qx + ql * 8, cx + cl * 8, cisp[cl], dots[ql * FDP + cl],
-                                     __fmul_rn(c[1], cvn[cl]), c[0], c[2], c[3], c[4], c[5], dl2, du2);
+                    pair_bounds_core(P, qx + ql * 8, cx + cl, cisp[cl], dots[ql * FDP + cl],
+                                     __fmul_rn(c[1], cvn[cl]), c[0], c[2], c[3], c[4], c[5], dl2, du2, FCB);
                     keep = dl2 <= tau2;
                 }
                 const unsigned mk = __ballot_sync(0xffffffffu, keep);
@@ -1969,10 +1987,10 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
     if (lane == 0 && P.evals && evals) atomicAdd((unsigned long long*)P.evals, (unsigned long long)evals);
 }
 
-// Job i of a unit: i < warm: warm-up (heap only) over the part's i-th level tile;
-// otherwise the part's (i - warm)-th tile, marked when warm-up already fed its heap.
-// The part's tiles are entries p, p + parts, ... of the tile's list (spiral, then
-// dataset tiles).
+// Job i of a unit: i < warm: warm-up (heap only) over the part's i-th spiral tile;
+// otherwise the part's (i - warm)-th tile, marked when its warm-up already fed its heap.
+// The part's main tiles are entries p, p + parts, ... of the tile's list (the level's
+// tiles in ascending order, then the dataset tiles).
 __global__ void gen_jobs_kernel(const JobUnit* __restrict__ units, Job* __restrict__ jobs) {
     const JobUnit U = units[blockIdx.x];
     for (int i = threadIdx.x; i < U.count; i += blockDim.x) {
@@ -1981,8 +1999,20 @@ __global__ void gen_jobs_kernel(const JobUnit* __restrict__ units, Job* __restri
         const int w = U.p + j * U.parts;
         int which, ctile;
         if (w < U.ntl) {
-            ctile = spiral_tile(U, w);
-            which = (warmup ? 2 : (j < U.warm ? 4 : 0)) | (U.fast_lvl ? 8 : 0);
+            if (warmup) {
+                ctile = spiral_tile(U, w);
+                which = 2;
+            } else {
+                ctile = main_tile(U, w);
+                // the part's own warm-up already fed this tile to its heaps
+                bool warmed = j < U.warm;
+                if (U.lin) {
+                    const int sw = spiral_index(U, ctile);
+                    warmed = sw >= U.p && (sw - U.p) % U.parts == 0 && (sw - U.p) / U.parts < U.warm;
+                }
+                which = warmed ? 4 : 0;
+            }
+            which |= U.fast_lvl ? 8 : 0;
         } else {
             ctile = U.lo_tile + (w - U.ntl);
             which = 1 | (ctile < U.ds_fast_end ? 8 : 0);
@@ -2522,6 +2552,11 @@ int ct_tree::knn_screened(const int64_t* q_ids, int64_t nq, int k, int predecess
             u.warm = warm; u.count = warm + mine; u.off = 0;
             u.fast_lvl = (sp.ntl > 0 && sp.lvl_size <= sp.min_q) ? 1 : 0;
             u.ds_fast_end = (int)std::min<long long>(sp.min_q / TC, (long long)INT_MAX);
+            // one-part calls sweep the level in ascending order after the warm-up (units of a
+            // level share its tiles in L2: 510 -> 422 GB of DRAM reads per sweep at N=262144);
+            // split calls keep the spiral (their trees fit in L2 and nearest-first order keeps
+            // their part thresholds tight)
+            u.lin = parts == 1 ? 1 : 0;
             units.push_back(u);
         }
     }

@@ -127,7 +127,7 @@ def estimate_tree_bytes(n: int, d: int, m: int) -> int:
 
 
 class ServingEngine:
-    def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 2, max_step_points: int = 16384,
+    def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 3, max_step_points: int = 16384,
                  max_step_work: float = 2.0e10, dense_pair_limit: float = 1.0e10, device=None,
                  reserve=(256, 3, 64), build_workers: int = 1):
         import torch

@@ -68,6 +68,7 @@ EXPORTED_SYMBOLS = (
     "ct_batch_order",
     "ct_luby_mis",
     "ct_tree_build_info",
+    "ct_tree_extend",
 )
 
 
@@ -127,6 +128,8 @@ def load(build_if_missing: bool = True):
         L.ct_build_residual.restype = ctypes.c_int
         L.ct_build_residual.argtypes = [vp, vp, vp, i64, i32, i32, f32, ctypes.POINTER(ctypes.c_float), i32, i32,
                                         i32, i32, u64, i32, vp, ctypes.POINTER(vp)]
+        L.ct_tree_extend.restype = ctypes.c_int
+        L.ct_tree_extend.argtypes = [vp, vp, vp, vp, i64, vp, ctypes.POINTER(vp)]
         L.ct_knn_residual.restype = ctypes.c_int
         L.ct_knn_residual.argtypes = [vp, vp, i64, i32, i32, i32, vp, vp, ctypes.POINTER(CtStats), vp]
         L.ct_knn_euclidean.restype = ctypes.c_int

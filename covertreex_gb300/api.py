@@ -147,6 +147,22 @@ def _resident_residual(coords: np.ndarray, ids: np.ndarray, *, seed: int, order:
     return _Resident("residual_correlation", ids, coords, index, seed, order)
 
 
+def _extend_residual(old: _Resident, new_coords: np.ndarray, new_ids: np.ndarray) -> _Resident:
+    """The residual tree with the configured backend's rows new_ids appended: a new device
+    handle grown from the old one (its rows copied on the device, its cover tree kept and
+    the new rows inserted), the old tree left valid."""
+    hb = get_residual_backend()
+    V = np.asarray(hb.v_matrix)
+    p = np.asarray(hb.p_diag).reshape(-1)
+    if new_ids.size and int(new_ids.max()) >= V.shape[0]:
+        raise ValueError(f"residual backend holds {V.shape[0]} rows; the tree needs index {int(new_ids.max())}")
+    kp = getattr(hb, "kernel_points_f32", None)
+    X = np.asarray(kp, dtype=np.float32)[new_ids] if kp is not None else new_coords
+    index = old.index.extend(V[new_ids], p[new_ids], X)
+    return _Resident("residual_correlation", np.concatenate([old.ids, new_ids]),
+                     np.concatenate([old.coords, new_coords], axis=0), index, old.seed, old.order)
+
+
 def _resident_euclidean(coords: np.ndarray, ids: np.ndarray, *, seed: int, order: str) -> _Resident:
     from .euclidean import EuclideanTree
 
@@ -211,7 +227,11 @@ class CoverTree:
         coords = np.concatenate([old.coords, new], axis=0)
         seed = self._seed(mis_seed) if mis_seed is not None else old.seed
         order = self._order(apply_batch_order) if apply_batch_order is not None else old.order
-        res = self._make(coords, ids, seed, order)
+        if old.metric == "residual_correlation" and seed == old.seed and order == old.order and new.shape[0]:
+            # the new rows go into a handle grown from the resident one (no rebuild)
+            res = _extend_residual(old, new, ids[old.n:])
+        else:
+            res = self._make(coords, ids, seed, order)
         out = CoverTree(runtime=self.runtime, tree=res)
         return (out, {"inserted": int(new.shape[0])}) if return_plan else out
 

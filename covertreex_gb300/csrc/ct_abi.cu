@@ -122,6 +122,51 @@ int ct_build_residual(const float* v, const float* p, const float* coords, int64
     return CT_OK;
 }
 
+int ct_tree_extend(const ct_tree* B, const float* v, const float* p, const float* coords, int64_t n_new, void* stream,
+                   ct_tree** out) {
+    if (!out) return fail(CT_ERR_ARG, "ct_tree_extend: out is NULL");
+    *out = nullptr;
+    if (!B) return fail(CT_ERR_ARG, "ct_tree_extend: base tree is NULL");
+    if (n_new < 0) return fail(CT_ERR_ARG, "ct_tree_extend: n_new < 0");
+    if (n_new > 0 && (!v || !p || !coords)) return fail(CT_ERR_ARG, "ct_tree_extend: NULL input pointer");
+    if (B->n + n_new > INT32_MAX) return fail(CT_ERR_UNSUPPORTED, "ct_tree_extend: more than 2^31 - 1 rows");
+    cudaStream_t st = (cudaStream_t)stream;
+    keep_pool_memory();
+    ct_tree* T = new (std::nothrow) ct_tree();
+    if (!T) return fail(CT_ERR_NOMEM, "ct_tree_extend: host allocation failed");
+    const long long nb = B->n, m = B->m, d = B->d;
+    T->n = nb + n_new; T->m = B->m; T->d = B->d; T->var = B->var; T->kernel_type = B->kernel_type;
+    T->chunk = B->chunk; T->order_mode = B->order_mode; T->seed = B->seed; T->slab_rows = B->slab_rows;
+    for (int i = 0; i < 64; ++i) T->inv_ls_host64[i] = B->inv_ls_host64[i];
+    int rc = T->alloc_metric();
+    if (rc != CT_OK) { const char* msg = T->err; int r = fail(rc, "ct_tree_extend: %s", msg); delete T; return r; }
+    // the base's rows and their derived data are copied on the device; only the new rows
+    // go through the metric setup
+    cudaError_t e = cudaMemcpyAsync(T->inv_ls, B->inv_ls, sizeof(float) * 64, cudaMemcpyDeviceToDevice, st);
+    auto D2D = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+    };
+    D2D(T->vnat, B->vnat, sizeof(float) * nb * m);
+    D2D(T->coords_raw, B->coords_raw, sizeof(float) * nb * d);
+    D2D(T->vperm, B->vperm, sizeof(float) * nb * m);
+    D2D(T->xs, B->xs, sizeof(float) * nb * d);
+    D2D(T->norms, B->norms, sizeof(float) * nb);
+    D2D(T->p, B->p, sizeof(float) * nb);
+    D2D(T->vnat + nb * m, v, sizeof(float) * n_new * m);
+    D2D(T->coords_raw + nb * d, coords, sizeof(float) * n_new * d);
+    if (e == cudaSuccess)
+        e = ct::launch_metric_setup(v, p, coords, n_new, (int)m, (int)d, T->inv_ls, T->vperm + nb * m, T->xs + nb * d,
+                                    T->norms + nb, T->p + nb, st);
+    if (e == cudaSuccess && B->has_tree) {
+        rc = T->grow_tree(B, st);
+        if (rc != CT_OK) { int r = fail(rc, "ct_tree_extend: tree: %s", T->err); delete T; return r; }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) { int r = cuda_fail(e, "ct_tree_extend"); delete T; return r; }
+    *out = T;
+    return CT_OK;
+}
+
 int ct_knn_residual(ct_tree* T, const int64_t* q_ids, int64_t nq, int32_t k, int32_t predecessor, int32_t form,
                     int64_t* out_idx, float* out_dist, ct_stats* stats, void* stream) {
     if (!T) return fail(CT_ERR_ARG, "ct_knn_residual: tree is NULL");

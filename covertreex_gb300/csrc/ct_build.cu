@@ -282,6 +282,15 @@ using namespace ct::treeb;
 static inline unsigned gridn(long long n, int b) { return (unsigned)((n + b - 1) / b); }
 
 int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_dataset*/, cudaStream_t st) {
+    return grow_tree(nullptr, st);
+}
+
+// base == nullptr: the build described at the top of this file.  Otherwise this handle
+// holds base's rows followed by new rows (ct_tree_extend): base's tree nodes keep their
+// node numbers, parents and levels, the new rows (ordered among themselves) follow them
+// and are inserted by the same prefix-doubling groups (the batch insert of the reference's
+// CoverTree.insert, api/pcct.py:171-197), and the tiny-p rows of both come last.
+int ct_tree::grow_tree(const ct_tree* base, cudaStream_t st) {
     const long long N = n;
     cudaError_t e = cudaSuccess;
     auto A = [&](void** ptr, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(ptr, bytes ? bytes : 16); };
@@ -299,34 +308,43 @@ int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_datase
     cudaEventRecord(ev0, st);
 
     // 1. node order: Hilbert (or natural), then rows with tiny p moved to the end
+    const long long nb = base ? base->n : 0;               // rows of the base handle
+    const long long n_tree_base = base ? base->n - base->n_side : 0;
+    const long long nr = N - nb;                           // rows ordered here
     int* order32 = nullptr;
-    A((void**)&order32, 4 * N);
-    if (e == cudaSuccess) {
+    A((void**)&order32, 4 * (nr > 0 ? nr : 1));
+    if (e == cudaSuccess && nr > 0) {
         if (order_mode == CT_ORDER_NATURAL) {
-            std::vector<int> id(N);
-            for (long long i = 0; i < N; ++i) id[i] = (int)i;
-            e = cudaMemcpyAsync(order32, id.data(), 4 * N, cudaMemcpyHostToDevice, st);
+            std::vector<int> id(nr);
+            for (long long i = 0; i < nr; ++i) id[i] = (int)i;
+            e = cudaMemcpyAsync(order32, id.data(), 4 * nr, cudaMemcpyHostToDevice, st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         } else {
-            e = ct::compute_order(coords_raw, N, d, (d == 3 && order_mode == CT_ORDER_MORTON) ? 2 : 1, order32, st);
+            e = ct::compute_order(coords_raw + (size_t)nb * d, nr, d, (d == 3 && order_mode == CT_ORDER_MORTON) ? 2 : 1,
+                                  order32, st);
         }
     }
-    std::vector<int> ord(N);
-    std::vector<float> ph(N);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ord.data(), order32, 4 * N, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(ph.data(), p, 4 * N, cudaMemcpyDeviceToHost, st);
+    std::vector<int> ord(nr > 0 ? nr : 1);
+    std::vector<float> ph(nr > 0 ? nr : 1);
+    std::vector<long long> bord(nb > 0 ? nb : 1);
+    if (e == cudaSuccess && nr > 0) e = cudaMemcpyAsync(ord.data(), order32, 4 * nr, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nr > 0) e = cudaMemcpyAsync(ph.data(), p + nb, 4 * nr, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && nb > 0) e = cudaMemcpyAsync(bord.data(), base->order, 8 * nb, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     std::vector<long long> ord64;
     n_side = 0;
     if (e == cudaSuccess) {
         ord64.reserve(N);
         const float pside = 1.f / (ct::kSideIsp * ct::kSideIsp);
-        for (long long i = 0; i < N; ++i) if (!(ph[ord[i]] < pside)) ord64.push_back(ord[i]);
+        for (long long i = 0; i < n_tree_base; ++i) ord64.push_back(bord[i]);
+        for (long long i = 0; i < nr; ++i) if (!(ph[ord[i]] < pside)) ord64.push_back(nb + ord[i]);
         const long long n_tree = (long long)ord64.size();
-        for (long long i = 0; i < N; ++i) if (ph[ord[i]] < pside) ord64.push_back(ord[i]);
+        for (long long i = n_tree_base; i < nb; ++i) ord64.push_back(bord[i]);
+        for (long long i = 0; i < nr; ++i) if (ph[ord[i]] < pside) ord64.push_back(nb + ord[i]);
         n_side = N - n_tree;
         e = cudaMemcpyAsync(order, ord64.data(), 8 * N, cudaMemcpyHostToDevice, st);
     }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // ord64 is a host buffer
     cudaFree(order32);
     const long long n_tree = N - n_side;
     if (e == cudaSuccess) {
@@ -343,6 +361,11 @@ int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_datase
         init_tree_kernel<<<gridn(N, 256), 256, 0, st>>>(N, parents, levels, (unsigned*)si, (unsigned*)si_up,
                                                         (unsigned*)sub_isp, tisp, sub_min, order);
         e = cudaGetLastError();
+    }
+    // the base tree's nodes keep their parents and levels (node numbers below n_tree_base)
+    if (e == cudaSuccess && n_tree_base > 0) {
+        e = cudaMemcpyAsync(parents, base->parents, 8 * n_tree_base, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(levels, base->levels, 4 * n_tree_base, cudaMemcpyDeviceToDevice, st);
     }
     // bound model of the tree: dataset maxima of ||v|| and of the scaled norms
     if (e == cudaSuccess) {
@@ -363,10 +386,11 @@ int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_datase
         e = cudaGetLastError();
     }
 
-    // 2. prefix-doubling groups over nodes [1, n_tree)
-    build_groups = 0;
-    build_conflict_edges = 0;
-    build_selected = 0;
+    // 2. prefix-doubling groups over nodes [1, n_tree) (over the new nodes [n_tree_base,
+    //    n_tree) when growing a base tree)
+    build_groups = base ? base->build_groups : 0;
+    build_conflict_edges = base ? base->build_conflict_edges : 0;
+    build_selected = base ? base->build_selected : 0;
     long long gmax = n_tree > 1 ? (n_tree - 1 + 1) / 2 + 1 : 1;
     long long *gq = nullptr, *t_idx = nullptr, *c_idx = nullptr, *indptr = nullptr, *indices = nullptr;
     float *t_d = nullptr, *c_d = nullptr, *w = nullptr;
@@ -381,14 +405,15 @@ int ct_tree::build_tree(const float* /*v_dataset*/, const float* /*coords_datase
     int smem_optin = 0, dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (e == cudaSuccess && n_tree > 0) {
+    if (e == cudaSuccess && n_tree > 0 && n_tree_base == 0) {
         set_root_kernel<<<1, 1, 0, st>>>(parents, levels);
         e = cudaGetLastError();
     }
     ct::BruteParams BP;
     BP.vperm = tvperm; BP.xs = txs; BP.norms = tnorms; BP.p = tp; BP.n = N; BP.m = m; BP.d = d;
     BP.kernel_type = kernel_type; BP.predecessor = 0; BP.var = var;
-    long long s = 1, size = 1;
+    long long s = n_tree_base > 0 ? n_tree_base : 1;
+    long long size = n_tree_base > 0 ? std::max<long long>(1, std::min(s, n_tree - s)) : 1;
     while (e == cudaSuccess && s < n_tree) {
         const long long g = std::min(size, n_tree - s);
         ++build_groups;

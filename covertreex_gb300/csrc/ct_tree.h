@@ -61,6 +61,7 @@ struct ct_tree {
 
     int alloc_metric();
     int build_tree(const float* v_dataset, const float* coords_dataset, cudaStream_t st);
+    int grow_tree(const ct_tree* base, cudaStream_t st);  // base's tree + this handle's extra rows
     int knn_tree(const int64_t* q_ids, int64_t nq, int k, int predecessor, int64_t* out_idx, float* out_dist,
                  ct_stats* stats, cudaStream_t st);
     // id_limit: query ids must lie in [0, id_limit) (default n; rows >= n are the query slab)

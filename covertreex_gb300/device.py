@@ -81,6 +81,40 @@ class CudaResidualIndex:
         self.build_params = {"chunk_size": int(chunk_size), "order": str(order), "seed": int(seed),
                              "build_tree": bool(build_tree), "query_slab": bool(query_slab)}
 
+    def extend(self, v_new, p_new, coords_new, *, stream=None) -> "CudaResidualIndex":
+        """A NEW index over this index's rows followed by the given rows (dataset ids n ..
+        n + len - 1), the counterpart of the reference's immutable ``CoverTree.insert``
+        (api/pcct.py:171-197): this index stays valid.  Existing rows are copied device to
+        device; a cover tree, if built, keeps its nodes and receives the new rows by
+        prefix-doubling group insertion (ct_tree_extend)."""
+        torch = _torch()
+        if self._h is None:
+            raise RuntimeError("index has been freed")
+        v = _as_device(v_new, torch.float32, self.device)
+        p = _as_device(p_new, torch.float32, self.device).reshape(-1)
+        c = _as_device(coords_new, torch.float32, self.device)
+        if c.dim() == 1:
+            c = c.reshape(-1, self.d)
+        b = int(p.shape[0])
+        if v.shape != (b, self.m) or c.shape != (b, self.d):
+            raise ValueError(f"new rows must be V [b, {self.m}], p [b] and coords [b, {self.d}]")
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().ct_tree_extend(self._h, v.data_ptr(), p.data_ptr(), c.data_ptr(), b,
+                                                  _stream_ptr(stream), ctypes.byref(h)))
+        out = CudaResidualIndex.__new__(CudaResidualIndex)
+        out.device = self.device
+        out.n, out.m, out.d = self.n + b, self.m, self.d
+        out.lengthscale = self.lengthscale
+        out.variance = self.variance
+        out.kernel_type = self.kernel_type
+        out.has_tree = self.has_tree
+        out._h = h
+        out.last_stats = {}
+        out.last_form = ""
+        out.build_params = dict(self.build_params)
+        return out
+
     # ------------------------------------------------------------------
     def knn_device(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense", stream=None,
                    out=None):

@@ -291,6 +291,19 @@ CT_API int ct_vfactor_chol(const ct_vfactor* f, double* l_out, void* stream);
 CT_API int ct_vfactor_free(ct_vfactor* f);
 
 /* Release a tree and its device memory. */
+/*
+ * A new handle over the base handle's rows followed by n_new new rows (v [n_new x m],
+ * p [n_new], coords [n_new x d]; device f32, the base's m, d and metric parameters):
+ * the counterpart of CoverTree.insert / CoverTreeWrapper.insert_residual
+ * (covertreex/api/pcct.py:171-197, src/lib.rs:254-321), whose trees are immutable, so
+ * the base stays valid.  The base's rows and derived data are copied device to device;
+ * when the base has a cover tree, its nodes keep their parents and levels and the new
+ * rows are inserted as prefix-doubling groups.  New rows get dataset ids base_n ..
+ * base_n + n_new - 1.  Every form answers exactly as a fresh build over all rows would.
+ */
+CT_API int ct_tree_extend(const ct_tree* base, const float* v, const float* p, const float* coords, int64_t n_new,
+                          void* stream, ct_tree** out);
+
 CT_API int ct_free(ct_tree* tree);
 
 #ifdef __cplusplus

@@ -54,13 +54,21 @@ def test_insert_then_delete_keep_dataset_numbering(cuda_available):
     configure_residual_correlation(hb)
     rt = _runtime()
     full = CoverTree(rt).fit(X, mis_seed=3)
-    part = CoverTree(rt).fit(X[:700], mis_seed=3).insert(X[700:])
-    assert part.num_points == 1200
+    first = CoverTree(rt).fit(X[:700], mis_seed=3)
+    part = first.insert(X[700:])  # a handle grown on the device from first's
+    assert part.num_points == 1200 and first.num_points == 700
     q = np.arange(0, 1200, 7, dtype=np.int64)
     for pred in (False, True):
         a = full.knn(q, k=8, predecessor_mode=pred, form="dense")
-        b = part.knn(q, k=8, predecessor_mode=pred, form="dense")
-        assert np.array_equal(a, b)
+        for form in ("dense", "tree", "screened"):
+            b = part.knn(q, k=8, predecessor_mode=pred, form=form)
+            assert np.array_equal(a, b) if form != "screened" else np.array_equal(
+                b, full.knn(q, k=8, predecessor_mode=pred, form="screened")), form
+    # trees are immutable: the tree inserted into still answers over its 700 rows
+    q7 = np.arange(0, 700, 9, dtype=np.int64)
+    ref7, _ = O.brute_knn_f32(hb.v_matrix[:700], hb.p_diag[:700], X[:700], 1.0, np.ones(3, np.float32), 0, q7, 8,
+                              True)
+    assert np.array_equal(first.knn(q7, k=8, predecessor_mode=True, form="tree"), ref7)
     gone = np.array([0, 5, 17, 333, 1199])
     smaller = full.delete(gone)
     assert smaller.num_points == 1200 - gone.size

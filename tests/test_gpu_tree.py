@@ -108,3 +108,41 @@ def test_traversal_natural_order_and_duplicates(cuda_available):
         di, dd = idx.knn(q, 20, predecessor=pred, form="dense")
         assert np.array_equal(ti, di)
         assert np.array_equal(td.view(np.uint32), dd.view(np.uint32))
+
+
+def test_extend_grows_the_tree_and_answers_as_a_fresh_build(cuda_available):
+    """ct_tree_extend (CoverTree.insert): a handle over the base's 3000 rows plus 1000
+    new ones (some of them tiny-p inducing rows, which join the side rows).  The base's
+    nodes keep their parents and levels; every form on the grown handle returns the
+    fresh build's rows bit for bit (the tree form through its certified prune); the base
+    still answers as before."""
+    case = gaussian_case(4000, 3, 64, 1, 1.0, seed=18)
+    n0 = 3000
+    base_case = dict(case, V=case["V"][:n0], p=case["p"][:n0], X=case["X"][:n0])
+    base = _tree_index(base_case)
+    fresh = _tree_index(case)
+    grown = base.extend(case["V"][n0:], case["p"][n0:], case["X"][n0:])
+    assert grown.n == 4000 and base.n == n0
+    tb, tg = base.tree_arrays(), grown.tree_arrays()
+    nt0 = n0 - base.build_info()["side_rows"]
+    assert np.array_equal(tg["node_to_dataset"][:nt0], tb["node_to_dataset"][:nt0])
+    assert np.array_equal(tg["parents"][:nt0], tb["parents"][:nt0])
+    assert np.array_equal(tg["levels"][:nt0], tb["levels"][:nt0])
+    assert np.array_equal(np.sort(tg["node_to_dataset"]), np.arange(4000))
+    side = case["p"][tg["node_to_dataset"]] < 1.0 / 1024
+    assert grown.build_info()["side_rows"] == side.sum()
+    assert np.all(tg["parents"][side] < 0)
+    q = np.arange(4000)
+    for pred in (True, False):
+        fi, fd = fresh.knn(q, 30, predecessor=pred, form="dense")
+        for form in ("dense", "tree", "screened"):
+            gi, gd = grown.knn(q, 30, predecessor=pred, form=form)
+            ri, rd = (fi, fd) if form != "screened" else fresh.knn(q, 30, predecessor=pred, form="screened")
+            assert np.array_equal(gi, ri), form
+            assert np.array_equal(gd.view(np.uint32), rd.view(np.uint32)), form
+    bi, bd = base.knn(np.arange(n0), 30, predecessor=True, form="tree")
+    oi, od = O.brute_knn_f32(base_case["V"], base_case["p"], base_case["X"], 1.0, base_case["ls"], 1,
+                             np.arange(n0), 30, True)
+    assert np.array_equal(bi, oi) and np.array_equal(bd.view(np.uint32), od.view(np.uint32))
+    for ix in (base, fresh, grown):
+        ix.free()

@@ -69,6 +69,7 @@ EXPORTED_SYMBOLS = (
     "ct_luby_mis",
     "ct_tree_build_info",
     "ct_tree_extend",
+    "ct_tree_subset",
 )
 
 
@@ -128,6 +129,8 @@ def load(build_if_missing: bool = True):
         L.ct_build_residual.restype = ctypes.c_int
         L.ct_build_residual.argtypes = [vp, vp, vp, i64, i32, i32, f32, ctypes.POINTER(ctypes.c_float), i32, i32,
                                         i32, i32, u64, i32, vp, ctypes.POINTER(vp)]
+        L.ct_tree_subset.restype = ctypes.c_int
+        L.ct_tree_subset.argtypes = [vp, vp, i64, vp, ctypes.POINTER(vp)]
         L.ct_tree_extend.restype = ctypes.c_int
         L.ct_tree_extend.argtypes = [vp, vp, vp, vp, i64, vp, ctypes.POINTER(vp)]
         L.ct_knn_residual.restype = ctypes.c_int

@@ -241,7 +241,12 @@ class CoverTree:
         keep = ~np.isin(old.ids, remove)
         if not keep.any():
             raise ValueError("delete would remove every point of the tree")
-        res = self._make(old.coords[keep], old.ids[keep], old.seed, old.order)
+        if old.metric == "residual_correlation":
+            # the kept rows are gathered on the device and the handle built from them
+            res = _Resident("residual_correlation", old.ids[keep], old.coords[keep],
+                            old.index.subset(np.nonzero(keep)[0]), old.seed, old.order)
+        else:
+            res = self._make(old.coords[keep], old.ids[keep], old.seed, old.order)
         out = CoverTree(runtime=self.runtime, tree=res)
         return (out, {"removed": int((~keep).sum())}) if return_plan else out
 

@@ -66,6 +66,23 @@ int batch_fail(const char* where, const char* msg, int code) { return fail(code,
         if (e_ != cudaSuccess) return cuda_fail(e_, where); \
     } while (0)
 
+namespace {
+// rows[i] of src (w floats per row) -> row i of dst
+__global__ void gather_f32_rows_kernel(const float* __restrict__ src, const int64_t* __restrict__ rows, long long n,
+                                       int w, float* __restrict__ dst) {
+    const long long total = n * (long long)w;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / w;
+        dst[e] = src[rows[r] * w + (e - r * w)];
+    }
+}
+__global__ void check_rows_kernel(const int64_t* __restrict__ rows, long long n, long long limit, int* __restrict__ bad) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n && (rows[i] < 0 || rows[i] >= limit || (i > 0 && rows[i] <= rows[i - 1]))) atomicOr(bad, 1);
+}
+}  // namespace
+
 extern "C" {
 
 int ct_version(void) { return 10000; }
@@ -120,6 +137,49 @@ int ct_build_residual(const float* v, const float* p, const float* coords, int64
     if (e != cudaSuccess) { int r = cuda_fail(e, "ct_build_residual"); delete T; return r; }
     *out = T;
     return CT_OK;
+}
+
+int ct_tree_subset(const ct_tree* B, const int64_t* rows, int64_t n_keep, void* stream, ct_tree** out) {
+    if (!out) return fail(CT_ERR_ARG, "ct_tree_subset: out is NULL");
+    *out = nullptr;
+    if (!B) return fail(CT_ERR_ARG, "ct_tree_subset: base tree is NULL");
+    if (n_keep <= 0) return fail(CT_ERR_ARG, "ct_tree_subset: n_keep must be positive");
+    if (!rows) return fail(CT_ERR_ARG, "ct_tree_subset: rows is NULL");
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long m = B->m, d = B->d;
+    float *v = nullptr, *p = nullptr, *c = nullptr;
+    int* bad = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&v, sizeof(float) * n_keep * m, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&p, sizeof(float) * n_keep, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&c, sizeof(float) * n_keep * d, st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&bad, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), st);
+    int hbad = 0;
+    if (e == cudaSuccess) {
+        check_rows_kernel<<<(unsigned)((n_keep + 255) / 256), 256, 0, st>>>(rows, n_keep, B->n, bad);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    int rc = CT_OK;
+    if (e == cudaSuccess && hbad) rc = fail(CT_ERR_ARG, "ct_tree_subset: rows must be ascending ids in [0, %lld)", (long long)B->n);
+    if (e == cudaSuccess && rc == CT_OK) {
+        gather_f32_rows_kernel<<<152 * 8, 256, 0, st>>>(B->vnat, rows, n_keep, (int)m, v);
+        gather_f32_rows_kernel<<<(unsigned)((n_keep + 255) / 256), 256, 0, st>>>(B->p, rows, n_keep, 1, p);
+        gather_f32_rows_kernel<<<(unsigned)((n_keep * d + 255) / 256), 256, 0, st>>>(B->coords_raw, rows, n_keep, (int)d, c);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && rc == CT_OK) {
+        // the base's lengthscales, recovered exactly from their inverses
+        float ls[64];
+        for (int i = 0; i < d; ++i) ls[i] = (float)(1.0 / B->inv_ls_host64[i]);
+        const int flags = (B->has_tree ? 0 : CT_BUILD_METRIC_ONLY) | (B->slab_rows > 0 ? CT_BUILD_QUERY_SLAB : 0);
+        rc = ct_build_residual(v, p, c, n_keep, (int32_t)m, (int32_t)d, B->var, ls, (int32_t)d, B->kernel_type,
+                               B->chunk, B->order_mode, B->seed, flags, stream, out);
+    }
+    cudaFreeAsync(v, st); cudaFreeAsync(p, st); cudaFreeAsync(c, st); cudaFreeAsync(bad, st);
+    if (e != cudaSuccess) return cuda_fail(e, "ct_tree_subset");
+    return rc;
 }
 
 int ct_tree_extend(const ct_tree* B, const float* v, const float* p, const float* coords, int64_t n_new, void* stream,

@@ -115,6 +115,31 @@ class CudaResidualIndex:
         out.build_params = dict(self.build_params)
         return out
 
+    def subset(self, rows, *, stream=None) -> "CudaResidualIndex":
+        """A NEW index over the given rows (ascending row numbers of this index), renumbered
+        0 .. len - 1: the counterpart of the reference's immutable ``CoverTree.delete``.
+        Rows are gathered on the device (ct_tree_subset); this index stays valid."""
+        torch = _torch()
+        if self._h is None:
+            raise RuntimeError("index has been freed")
+        r = _as_device(np.asarray(rows, dtype=np.int64).reshape(-1), torch.int64, self.device)
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.load().ct_tree_subset(self._h, r.data_ptr(), int(r.shape[0]), _stream_ptr(stream),
+                                                  ctypes.byref(h)))
+        out = CudaResidualIndex.__new__(CudaResidualIndex)
+        out.device = self.device
+        out.n, out.m, out.d = int(r.shape[0]), self.m, self.d
+        out.lengthscale = self.lengthscale
+        out.variance = self.variance
+        out.kernel_type = self.kernel_type
+        out.has_tree = self.has_tree
+        out._h = h
+        out.last_stats = {}
+        out.last_form = ""
+        out.build_params = dict(self.build_params)
+        return out
+
     # ------------------------------------------------------------------
     def knn_device(self, q_ids, k: int, *, predecessor: bool = False, form: str = "dense", stream=None,
                    out=None):

@@ -304,6 +304,14 @@ CT_API int ct_vfactor_free(ct_vfactor* f);
 CT_API int ct_tree_extend(const ct_tree* base, const float* v, const float* p, const float* coords, int64_t n_new,
                           void* stream, ct_tree** out);
 
+/*
+ * A new handle over the base's rows `rows` (device int64, ascending, in [0, base n)),
+ * renumbered 0 .. n_keep - 1: the counterpart of CoverTree.delete (covertreex/api/pcct.py:
+ * 199-220, algo/batch_delete.py), immutable like it.  The rows are gathered on the device
+ * and the handle (and its cover tree, when the base has one) is built from them.
+ */
+CT_API int ct_tree_subset(const ct_tree* base, const int64_t* rows, int64_t n_keep, void* stream, ct_tree** out);
+
 CT_API int ct_free(ct_tree* tree);
 
 #ifdef __cplusplus

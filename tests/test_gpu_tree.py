@@ -146,3 +146,27 @@ def test_extend_grows_the_tree_and_answers_as_a_fresh_build(cuda_available):
     assert np.array_equal(bi, oi) and np.array_equal(bd.view(np.uint32), od.view(np.uint32))
     for ix in (base, fresh, grown):
         ix.free()
+
+
+def test_subset_answers_as_a_fresh_build(cuda_available):
+    """ct_tree_subset (CoverTree.delete): rows gathered on the device give a handle whose
+    every form returns the rows of a fresh build over the same rows, bit for bit; bad
+    row lists are rejected."""
+    from covertreex_gb300.device import CudaResidualIndex
+
+    case = gaussian_case(3000, 3, 64, 0, 1.5, seed=27)
+    base = _tree_index(case)
+    keep = np.setdiff1d(np.arange(3000), np.random.default_rng(28).choice(3000, 400, replace=False))
+    sub = base.subset(keep)
+    fresh = _tree_index(dict(case, V=case["V"][keep], p=case["p"][keep], X=case["X"][keep]))
+    q = np.arange(keep.size)
+    for form in ("dense", "tree", "screened"):
+        a, ad = sub.knn(q, 20, predecessor=True, form=form)
+        b, bd = fresh.knn(q, 20, predecessor=True, form=form)
+        assert np.array_equal(a, b) and np.array_equal(ad.view(np.uint32), bd.view(np.uint32)), form
+    with pytest.raises(Exception):
+        base.subset(np.array([5, 3]))          # not ascending
+    with pytest.raises(Exception):
+        base.subset(np.array([0, 3000]))       # out of range
+    for ix in (base, sub, fresh):
+        ix.free()

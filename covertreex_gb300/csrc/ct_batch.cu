@@ -222,6 +222,7 @@ struct ct_batch {
     // device and pinned buffers
     unsigned char* d_desc = nullptr;
     unsigned char* h_desc = nullptr;
+    std::vector<unsigned char*> old_pinned;  // replaced pinned descriptor buffers, freed with the batch
     size_t desc_cap = 0;
     unsigned long long* d_ctr = nullptr;
     int* d_done = nullptr;
@@ -254,6 +255,7 @@ struct ct_batch {
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (d_desc) cudaFree(d_desc);
         if (h_desc) cudaFreeHost(h_desc);
+        for (unsigned char* h : old_pinned) cudaFreeHost(h);
         if (d_ctr) cudaFree(d_ctr);
         if (d_done) cudaFree(d_done);
         if (d_part) cudaFree(d_part);
@@ -371,35 +373,43 @@ void make_plan(const ct_batch* B, int qt, int cps, int ips, Plan& P) {
     P.done_ints = done_off;
 }
 
-int ensure_capacity(ct_batch* B, const Plan& P) {
+// Growth is stream-ordered: the old buffers are released on the run's stream after the
+// previous run (its staging event), the new ones come from the stream-ordered allocator,
+// so a growing batch never synchronises the device (a serving step would otherwise wait
+// for every build and screened request in flight).  Old pinned descriptor buffers are kept
+// until the batch is freed (freeing pinned memory synchronises).
+int ensure_capacity(ct_batch* B, const Plan& P, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
     const size_t need_desc = kHeaderBytes + sizeof(Problem) * std::max<size_t>(P.probs.size(), 1);
+    const bool grow = need_desc > B->desc_cap || P.part_bytes > B->part_cap || P.done_ints > B->done_cap;
+    if (grow && B->staged_pending) e = cudaStreamWaitEvent(st, B->staged, 0);
+    if (e != cudaSuccess) return B->cuda_err(e, "ct_batch: ordering a buffer growth");
     if (need_desc > B->desc_cap) {
-        if (B->staged_pending) cudaEventSynchronize(B->staged);
+        if (B->staged_pending) cudaEventSynchronize(B->staged);  // the pinned buffer's last copy
         B->staged_pending = false;
         size_t cap = std::max<size_t>(need_desc * 2, 16384);
-        if (B->d_desc) cudaFree(B->d_desc);
-        if (B->h_desc) cudaFreeHost(B->h_desc);
+        if (B->d_desc) cudaFreeAsync(B->d_desc, st);
+        if (B->h_desc) B->old_pinned.push_back(B->h_desc);
         B->d_desc = nullptr; B->h_desc = nullptr; B->desc_cap = 0;
-        e = cudaMalloc((void**)&B->d_desc, cap);
+        e = cudaMallocAsync((void**)&B->d_desc, cap, st);
         if (e == cudaSuccess) e = cudaMallocHost((void**)&B->h_desc, cap);
         if (e != cudaSuccess) return B->cuda_err(e, "ct_batch: descriptor buffers");
         B->desc_cap = cap;
     }
     if (P.part_bytes > B->part_cap) {
-        if (B->d_part) cudaFree(B->d_part);
+        if (B->d_part) cudaFreeAsync(B->d_part, st);
         B->d_part = nullptr; B->part_cap = 0;
-        e = cudaMalloc((void**)&B->d_part, P.part_bytes);
+        const size_t cap = std::max<size_t>(P.part_bytes * 2, (size_t)1 << 20);
+        e = cudaMallocAsync((void**)&B->d_part, cap, st);
         if (e != cudaSuccess) return B->cuda_err(e, "ct_batch: partial-list scratch");
-        B->part_cap = P.part_bytes;
+        B->part_cap = cap;
     }
     if (P.done_ints > B->done_cap) {
-        if (B->d_done) cudaFree(B->d_done);
+        if (B->d_done) cudaFreeAsync(B->d_done, st);
         B->d_done = nullptr; B->done_cap = 0;
         const size_t cap = std::max<size_t>(P.done_ints * 2, 4096);
-        e = cudaMalloc((void**)&B->d_done, cap * sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(B->d_done, 0, cap * sizeof(int));
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        e = cudaMallocAsync((void**)&B->d_done, cap * sizeof(int), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B->d_done, 0, cap * sizeof(int), st);
         if (e != cudaSuccess) return B->cuda_err(e, "ct_batch: tile counters");
         B->done_cap = cap;
     }
@@ -413,7 +423,7 @@ int run_shape(ct_batch* B, int qt, int cps, int ips, bool use_graph, cudaStream_
     B->last_pairs = P.pairs;
     B->last_qt = qt; B->last_cps = cps; B->last_ips = ips;
     if (P.total_items == 0) return CT_OK;
-    int rc = ensure_capacity(B, P);
+    int rc = ensure_capacity(B, P, st);
     if (rc != CT_OK) return rc;
     for (Problem& pr : P.probs) {
         if (pr.split > 1) {

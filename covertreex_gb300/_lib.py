@@ -38,6 +38,7 @@ FORMS = {"dense": CT_FORM_DENSE, "tree": CT_FORM_TREE, "screened": CT_FORM_SCREE
 EXPORTED_SYMBOLS = (
     "ct_version",
     "ct_set_timing",
+    "ct_set_cta_budget",
     "ct_last_error",
     "ct_build_residual",
     "ct_knn_residual",
@@ -124,6 +125,8 @@ def load(build_if_missing: bool = True):
         L.ct_version.argtypes = []
         L.ct_set_timing.restype = ctypes.c_int
         L.ct_set_timing.argtypes = [ctypes.c_int]
+        L.ct_set_cta_budget.restype = ctypes.c_int
+        L.ct_set_cta_budget.argtypes = [ctypes.c_int32]
         L.ct_last_error.restype = ctypes.c_char_p
         L.ct_last_error.argtypes = []
         L.ct_build_residual.restype = ctypes.c_int

@@ -25,6 +25,7 @@ namespace {
 
 thread_local char g_last_error[512] = "";
 thread_local bool g_timing = false;
+thread_local int g_cta_budget = 0;  // cap on the grid of the FP64 embed kernels (0 = none)
 
 int fail(int code, const char* fmt, ...) {
     va_list ap;
@@ -89,6 +90,12 @@ int ct_version(void) { return 10000; }
 
 int ct_set_timing(int enable) {
     g_timing = enable != 0;
+    return CT_OK;
+}
+
+int ct_set_cta_budget(int32_t ctas) {
+    if (ctas < 0) return fail(CT_ERR_ARG, "ct_set_cta_budget: ctas < 0");
+    g_cta_budget = ctas;
     return CT_OK;
 }
 
@@ -523,7 +530,7 @@ int ct_vfactor_embed(ct_vfactor* F, const double* x, int64_t n, float* v_out, fl
     if (e == cudaSuccess) e = cudaMallocAsync((void**)&vc, sizeof(double) * (size_t)chunk * F->m, st);
     if (e == cudaSuccess)
         e = ct::vmatrix_embed(x, n, F->d, F->z, F->m, F->kernel_type, F->variance, F->lengthscale, F->Li, kc, vc,
-                              chunk, v_out, p_out, st, nullptr);
+                              chunk, v_out, p_out, st, nullptr, g_cta_budget);
     if (kc) cudaFreeAsync(kc, st);
     if (vc) cudaFreeAsync(vc, st);
     if (e != cudaSuccess) return cuda_fail(e, "ct_vfactor_embed");

@@ -156,28 +156,27 @@ __global__ void __launch_bounds__(128) trinv_kernel(const double* __restrict__ L
     for (int i = lane; i < m; i += 32) Li[(size_t)i * m + c] = x[i];
 }
 
-// Kc[r][t] = K(x_{r0+r}, z_t) for r < rows.
+// Kc[r][t] = K(x_{r0+r}, z_t) for r < rows (grid-stride: the grid may be capped).
 __global__ void kxm_kernel(const double* __restrict__ x, long long r0, long long rows, const double* __restrict__ z,
                            int m, int d, int kt, double var, double ls, double* __restrict__ Kc) {
-    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (e >= rows * m) return;
-    const long long r = e / m;
-    const int t = (int)(e - r * m);
-    Kc[e] = kernel_f64(x + (size_t)(r0 + r) * d, z + (size_t)t * d, d, kt, var, ls);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < rows * m;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long r = e / m;
+        const int t = (int)(e - r * m);
+        Kc[e] = kernel_f64(x + (size_t)(r0 + r) * d, z + (size_t)t * d, d, kt, var, ls);
+    }
 }
 
-// Vc[r][j] = sum_{t <= j} Kc[r][t] Li[j][t]; 32 x 32 tile, 256 threads, 2 x 2 each.  The
-// small tile keeps each block short (GB300's FP64 rate is low): a serving build's blocks
-// then free their SMs quickly for the query kernels on higher-priority streams.
+// Vc[r][j] = sum_{t <= j} Kc[r][t] Li[j][t]; 32 x 32 tiles, 256 threads, 2 x 2 each, a
+// block looping over tiles when the grid is capped.  GB300's FP64 rate is low (one block
+// of eight warps fills an SM's FP64 pipe), so a serving build runs these kernels on a
+// capped grid (ct_set_cta_budget): the other SMs stay free of build blocks, whose shared
+// memory would keep the screened form's large blocks off an SM.
 constexpr int GT = 32;
 constexpr int GK = 32;
-__global__ void __launch_bounds__(256) dgemm_lt_kernel(const double* __restrict__ Kc, long long rows,
-                                                       const double* __restrict__ Li, int m,
-                                                       double* __restrict__ Vc) {
-    __shared__ double As[GK][GT + 1];
-    __shared__ double Bs[GK][GT + 1];
-    const long long r0 = (long long)blockIdx.y * GT;
-    const int j0 = blockIdx.x * GT;
+__device__ __forceinline__ void dgemm_lt_tile(const double* __restrict__ Kc, long long rows,
+                                              const double* __restrict__ Li, int m, double* __restrict__ Vc,
+                                              double (*As)[GT + 1], double (*Bs)[GT + 1], long long r0, int j0) {
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     double acc[2][2];
 #pragma unroll
@@ -220,6 +219,17 @@ __global__ void __launch_bounds__(256) dgemm_lt_kernel(const double* __restrict_
             if (j < m) Vc[row * m + j] = acc[u][w];
         }
     }
+}
+
+__global__ void __launch_bounds__(256) dgemm_lt_kernel(const double* __restrict__ Kc, long long rows,
+                                                       const double* __restrict__ Li, int m,
+                                                       double* __restrict__ Vc) {
+    __shared__ double As[GK][GT + 1];
+    __shared__ double Bs[GK][GT + 1];
+    const int tiles_j = (m + GT - 1) / GT;
+    const long long tiles = tiles_j * ((rows + GT - 1) / GT);
+    for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x)  // grid-stride: the grid may be capped
+        dgemm_lt_tile(Kc, rows, Li, m, Vc, As, Bs, (tile / tiles_j) * GT, (int)(tile % tiles_j) * GT);
 }
 
 // One warp per row: p = max(var - ||v||^2, 1e-9) in FP64 (fixed summation order),
@@ -286,14 +296,18 @@ long long vmatrix_chunk_rows(long long n, int m) {
 
 cudaError_t vmatrix_embed(const double* x, long long n, int d, const double* z, int m, int kt, double var, double ls,
                           const double* Li, double* kc, double* vc, long long chunk, float* V, float* p,
-                          cudaStream_t st, int* launches) {
+                          cudaStream_t st, int* launches, int max_ctas) {
     int nl = 0;
+    auto capped = [&](long long blocks) {
+        if (max_ctas > 0 && blocks > max_ctas) blocks = max_ctas;
+        return (unsigned)(blocks > 0 ? blocks : 1);
+    };
     for (long long r0 = 0; r0 < n; r0 += chunk) {
         const long long rows = n - r0 < chunk ? n - r0 : chunk;
         const long long el = rows * m;
-        kxm_kernel<<<(unsigned)((el + 255) / 256), 256, 0, st>>>(x, r0, rows, z, m, d, kt, var, ls, kc);
-        dim3 grid((unsigned)((m + GT - 1) / GT), (unsigned)((rows + GT - 1) / GT));
-        dgemm_lt_kernel<<<grid, 256, 0, st>>>(kc, rows, Li, m, vc);
+        kxm_kernel<<<capped((el + 255) / 256), 256, 0, st>>>(x, r0, rows, z, m, d, kt, var, ls, kc);
+        const long long tiles = (long long)((m + GT - 1) / GT) * ((rows + GT - 1) / GT);
+        dgemm_lt_kernel<<<capped(tiles), 256, 0, st>>>(kc, rows, Li, m, vc);
         finalize_rows_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, st>>>(vc, rows, m, var, V + r0 * m,
                                                                                p + r0);
         nl += 3;

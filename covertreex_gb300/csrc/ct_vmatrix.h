@@ -14,10 +14,11 @@ cudaError_t vmatrix_factor(const double* z, int m, int d, int kt, double var, do
 // at most about 256 MB each).
 long long vmatrix_chunk_rows(long long n, int m);
 
-// V [n x m] f32 and p [n] f32 for points x [n x d] (device FP64).
+// V [n x m] f32 and p [n] f32 for points x [n x d] (device FP64).  max_ctas > 0 caps the
+// grid of the kernel-matrix and GEMM kernels (their blocks then loop).
 cudaError_t vmatrix_embed(const double* x, long long n, int d, const double* z, int m, int kt, double var, double ls,
                           const double* Li, double* kc, double* vc, long long chunk, float* V, float* p,
-                          cudaStream_t st, int* launches);
+                          cudaStream_t st, int* launches, int max_ctas = 0);
 
 }  // namespace ct
 

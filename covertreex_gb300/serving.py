@@ -129,7 +129,7 @@ def estimate_tree_bytes(n: int, d: int, m: int) -> int:
 class ServingEngine:
     def __init__(self, *, hbm_budget_bytes: float = 120e9, slots: int = 3, max_step_points: int = 16384,
                  max_step_work: float = 2.0e10, dense_pair_limit: float = 1.0e10, device=None,
-                 reserve=(256, 3, 64), build_workers: int = 1):
+                 reserve=(256, 3, 64), build_workers: int = 1, build_ctas: int = 0):
         import torch
 
         from .device import CudaBatch
@@ -142,6 +142,7 @@ class ServingEngine:
         self.max_step_points = int(max_step_points)
         self.max_step_work = float(max_step_work)         # sum of Q * N * m per dense step
         self.dense_pair_limit = float(dense_pair_limit)   # Q * N * m at or below which a query runs dense
+        self.build_ctas = int(build_ctas)                 # grid cap of a build's FP64 embed (0 = none)
         self.trees: Dict[int, ResidentTree] = {}
         self.used_bytes = 0
         self.reserved_bytes = 0
@@ -199,6 +200,12 @@ class ServingEngine:
         return ResidentTree(req.rid, index, f, n, d, index.m, nbytes, time.perf_counter() - t0)
 
     def _build_worker(self, st):
+        from . import _lib
+
+        # optionally the FP64 embed of a build runs on a capped grid, so that most SMs stay
+        # free of build blocks (measured: a cap of 48 blocks slows builds enough that queries
+        # wait for their trees at 500 req/s, so the default is no cap)
+        _lib.check(_lib.load().ct_set_cta_budget(int(self.build_ctas)))
         while True:
             item = self._build_in.get()
             if item is None:

@@ -94,6 +94,13 @@ CT_API int ct_version(void);
  * returning and fills the *_ms fields of ct_stats.  No counterpart in the reference. */
 CT_API int ct_set_timing(int enable);
 
+/* Cap (per calling thread) on the number of thread blocks of the FP64 kernel-matrix and
+ * GEMM kernels of ct_vfactor_embed; 0 (the default) = no cap.  A serving loop sets it in
+ * its build thread: with GB300's low FP64 rate a few blocks per SM already fill the FP64
+ * pipe, and the SMs left free of build blocks stay available to query kernels (a
+ * trade against build latency: the serving engine leaves it off by default). */
+CT_API int ct_set_cta_budget(int32_t ctas);
+
 /* Message of the calling thread's last failure ("" if none). */
 CT_API const char* ct_last_error(void);
 

@@ -176,6 +176,37 @@ __device__ __forceinline__ void heap_push(float* h, int n, float x) {
 // bit 2 of `which`: a kept job whose candidate tile already fed the heap during warm-up
 __device__ __forceinline__ bool jb_warm_seen(const Job& jb) { return (jb.which & 4) != 0; }
 
+// Squared scaled distance and kernel value of one query with two staged candidates
+// (columns .x and .y of the record pair r4), every operation explicitly rounded so that
+// the epilogue's tiers see the same bits for a pair.  Matern also returns a = sqrt(5 d2)
+// and e^-a for the error term.
+template <int DP, int KT>
+__device__ __forceinline__ void pair_kv2(const float4* r4, const float (&nxq)[kMaxD], float var, float2& d2,
+                                         float2& kv, float2& a, float2& ea) {
+    d2 = make_float2(0.f, 0.f);
+    float2 t;
+#pragma unroll
+    for (int h = 0; h < DP / 2; ++h) {
+        const float4 x = r4[h];
+        t = __fadd2_rn(make_float2(x.x, x.y), make_float2(nxq[2 * h], nxq[2 * h]));
+        d2 = __ffma2_rn(t, t, d2);
+        t = __fadd2_rn(make_float2(x.z, x.w), make_float2(nxq[2 * h + 1], nxq[2 * h + 1]));
+        d2 = __ffma2_rn(t, t, d2);
+    }
+    if (KT == 0) {
+        const float2 h = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);
+        kv = __fmul2_rn(make_float2(var, var), make_float2(__expf(h.x), __expf(h.y)));
+        a = ea = make_float2(0.f, 0.f);
+    } else {
+        a = __fmul2_rn(make_float2(2.2360679775f, 2.2360679775f), make_float2(sqrtf(d2.x), sqrtf(d2.y)));
+        ea = make_float2(__expf(-a.x), __expf(-a.y));
+        // var (1 + a + a^2 / 3) e^-a, each step rounded
+        const float2 a2 = __fmul2_rn(__fmul2_rn(a, a), make_float2(0.33333334f, 0.33333334f));
+        const float2 poly = __fadd2_rn(__fadd2_rn(make_float2(1.f, 1.f), a), a2);
+        kv = __fmul2_rn(__fmul2_rn(make_float2(var, var), poly), ea);
+    }
+}
+
 // DP: coordinates read per candidate (4 when D <= 4, else 8).  KT: kernel type (0 RBF,
 // 1 Matern 5/2) as a template parameter, so each group of 8 pairs is one basic block.
 template <int MODE, int DP, int KT>
@@ -512,6 +543,22 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     for (int i = 0; i < 8; ++i) rmax = fmaxf(rmax, fmaxf(kmax - v[i], v[i]));
                     const float ghi = (rmax * (1.f + 3e-7f) + vnq * gr[0] + ekmax + 1e-30f) * gr[1] * (1.f + 1e-6f);
                     if (!(ghi >= thr_keep)) continue;
+                    // Second tier: each pair's kernel value, computed exactly as phase 1 does,
+                    // gives phase 1's R = |kv - s| bit for bit; with the group's largest error
+                    // term and 1/sqrt(p) as above, rc bounds phase 1's survivor bound of every
+                    // pair.  Near candidates pass the box test (the box cannot see that s
+                    // tracks kv) but rarely this one; it costs about half of phase 1.
+                    float rc = 0.f;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const float4* r4 = (const float4*)(rb + ((col0 >> 1) + i) * (2 * REC));
+                        float2 d2, kv, am, ea;
+                        pair_kv2<DP, KT>(r4, nxq, P.var, d2, kv, am, ea);
+                        const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
+                        rc = fmaxf(rc, fmaxf(fabsf(dif.x), fabsf(dif.y)));
+                    }
+                    const float gc = (rc * (1.f + 3e-7f) + vnq * gr[0] + ekmax + 1e-30f) * gr[1] * (1.f + 1e-6f);
+                    if (!(gc >= thr_keep)) continue;
                 }
                 // Phase 1, no stores: certified bounds of the group's 8 pairs, as
                 //   blo = (R - e) * isc (heap test)  and  bhi = (R + e) * isc (survivor test),
@@ -529,28 +576,15 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                         const float4 m0 = r4[4];  // err_coef * |v_c|, 1/sqrt(p_c)
                         const float4 m1 = r4[5];  // 2.4e-7 max|x_c| (unused), id
                         const float2 err = make_float2(m0.x, m0.y), isc = make_float2(m0.z, m0.w);
-                        float2 d2 = make_float2(0.f, 0.f), t;
-#pragma unroll
-                        for (int h = 0; h < DP / 2; ++h) {
-                            const float4 x = r4[h];
-                            t = __fadd2_rn(make_float2(x.x, x.y), make_float2(nxq[2 * h], nxq[2 * h]));
-                            d2 = __ffma2_rn(t, t, d2);
-                            t = __fadd2_rn(make_float2(x.z, x.w), make_float2(nxq[2 * h + 1], nxq[2 * h + 1]));
-                            d2 = __ffma2_rn(t, t, d2);
-                        }
-                        float2 kv, ek;
+                        float2 d2, kv, ek, am, ea;
+                        pair_kv2<DP, KT>(r4, nxq, P.var, d2, kv, am, ea);
                         if (KT == 0) {
-                            const float2 h = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);
-                            kv = __fmul2_rn(make_float2(P.var, P.var), make_float2(__expf(h.x), __expf(h.y)));
                             ek = __fmul2_rn(kv, __ffma2_rn(make_float2(alk, alk), d2, make_float2(bek, bek)));
                         } else {
                             const float2 ed2 = __ffma2_rn(make_float2(ale, ale), d2, make_float2(bee, bee));
-                            const float aa = 2.2360679775f * sqrtf(d2.x), ab = 2.2360679775f * sqrtf(d2.y);
-                            const float ea = __expf(-aa), eb = __expf(-ab);
-                            kv.x = P.var * (1.f + aa + aa * aa * 0.33333334f) * ea;
-                            kv.y = P.var * (1.f + ab + ab * ab * 0.33333334f) * eb;
-                            ek.x = kv.x * (1e-6f + 2.4e-7f * aa) + P.var * (0.8334f * ed2.x + 1e-7f * aa * aa) * (1.f + aa) * ea;
-                            ek.y = kv.y * (1e-6f + 2.4e-7f * ab) + P.var * (0.8334f * ed2.y + 1e-7f * ab * ab) * (1.f + ab) * eb;
+                            const float aa = am.x, ab = am.y;
+                            ek.x = kv.x * (1e-6f + 2.4e-7f * aa) + P.var * (0.8334f * ed2.x + 1e-7f * aa * aa) * (1.f + aa) * ea.x;
+                            ek.y = kv.y * (1e-6f + 2.4e-7f * ab) + P.var * (0.8334f * ed2.y + 1e-7f * ab * ab) * (1.f + ab) * ea.y;
                         }
                         const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
                         const float2 R = make_float2(fabsf(dif.x), fabsf(dif.y));

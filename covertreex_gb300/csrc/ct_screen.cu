@@ -609,16 +609,18 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     }
                 };
                 if (fast_ids) phase1(std::false_type{}); else phase1(std::true_type{});
-                // Phase 2: survivors and heap against the current thresholds.  Phase 1's
-                // values do not depend on the thresholds, so this keeps and heaps exactly
-                // the pairs that pair-by-pair processing would.  Most groups have no pair
-                // to keep or heap; one test skips them (the thresholds then stay as they are).
-                // (the group's largest bounds decide: fmaxf skips the NaN of padding rows)
+                // Phase 2: survivors and heap against the thresholds as they stand at the
+                // group's start.  Most groups have no pair to keep or heap; one test skips
+                // them.  (The group's largest bounds decide: fmaxf skips the NaN of padding
+                // rows.)  Keeping against the group's starting threshold keeps at least the
+                // pairs that a threshold lowered within the group would; every kept pair
+                // still satisfies dl2 <= tau^2 for a valid tau.
                 float mh = bhi[0], ml = blo[0];
 #pragma unroll
                 for (int i = 1; i < 8; ++i) { mh = fmaxf(mh, bhi[i]); ml = fmaxf(ml, blo[i]); }
                 const bool any = (keep_job & (mh >= thr_keep)) | (feed_heap & (ml > thr_heap));
                 if (!any) continue;
+                unsigned hmask = 0;  // pairs of the group that may lower the heap's top
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     if (keep_job && bhi[i] >= thr_keep) {
@@ -626,15 +628,30 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                             P.surv[((size_t)slot * 2 + half) * P.half_cap + cnt] = bid[i];
                             P.survb[((size_t)slot * 2 + half) * P.half_cap + cnt] = bhi[i];
                         }
-                        if (++cnt > P.half_cap) {
-                            ovf = true;
-                            thr_keep = __int_as_float(0x7f800000);
-                            thr_heap = __int_as_float(0x7f800000);
-                        }
+                        ++cnt;
                     }
-                    if (feed_heap && blo[i] > thr_heap) {
+                    if (feed_heap && blo[i] > thr_heap) hmask |= 1u << i;
+                }
+                if (cnt > P.half_cap) {
+                    // overflowed: the row stops keeping and heaping
+                    ovf = true;
+                    thr_keep = __int_as_float(0x7f800000);
+                    thr_heap = __int_as_float(0x7f800000);
+                    hmask = 0;
+                }
+                // Heap updates one pending pair per iteration: the warp runs as many rounds as
+                // its busiest lane has pairs, not one round per pair position that any lane
+                // needs.  A pair whose bound no longer beats the top (lowered by an earlier
+                // pair of the group) is dropped by the top test.
+                while (hmask) {
+                    const int pi = __ffs(hmask) - 1;
+                    hmask &= hmask - 1u;
+                    float b = blo[0];
+#pragma unroll
+                    for (int i = 1; i < 8; ++i) b = pi == i ? blo[i] : b;
+                    {
                         // exact certified upper bound of d^2 for this pair (0 for the query itself)
-                        const float du2 = 1.f - fminf(fmaxf(blo[i], 0.f) * isq * (1.f - 1e-6f), 1.f);
+                        const float du2 = 1.f - fminf(fmaxf(b, 0.f) * isq * (1.f - 1e-6f), 1.f);
                         bool changed = false;
                         if (hn < P.k) {
                             heap_push(heap, hn, du2);

@@ -148,16 +148,27 @@ __host__ __device__ inline SmemLayout smem_layout(int k, int nstages) {
     return L;
 }
 
-// Max-heap of floats stored strided (element i of thread t at h[i * kEpiThreads]).
+// Four-ary max-heap of floats stored strided (element i of thread t at h[i * kEpiThreads];
+// children of i at 4i+1 .. 4i+4).  Three levels hold up to 85 elements, and the four child
+// loads of a level are independent, so a sift costs about one shared-memory latency a level.
 __device__ __forceinline__ void heap_sift_down(float* h, int n, float x) {
     int i = 0;
     for (;;) {
-        int l = 2 * i + 1;
-        if (l >= n) break;
-        int r = l + 1;
-        int c = (r < n && h[r * kEpiThreads] > h[l * kEpiThreads]) ? r : l;
-        if (h[c * kEpiThreads] <= x) break;
-        h[i * kEpiThreads] = h[c * kEpiThreads];
+        const int c0 = 4 * i + 1;
+        if (c0 >= n) break;
+        const float ninf = __int_as_float(0xff800000);
+        const float a0 = h[c0 * kEpiThreads];
+        const float a1 = c0 + 1 < n ? h[(c0 + 1) * kEpiThreads] : ninf;
+        const float a2 = c0 + 2 < n ? h[(c0 + 2) * kEpiThreads] : ninf;
+        const float a3 = c0 + 3 < n ? h[(c0 + 3) * kEpiThreads] : ninf;
+        const bool s01 = a1 > a0, s23 = a3 > a2;
+        const float m01 = s01 ? a1 : a0, m23 = s23 ? a3 : a2;
+        const int i01 = s01 ? c0 + 1 : c0, i23 = s23 ? c0 + 3 : c0 + 2;
+        const bool hi = m23 > m01;
+        const float mc = hi ? m23 : m01;
+        const int c = hi ? i23 : i01;
+        if (mc <= x) break;
+        h[i * kEpiThreads] = mc;
         i = c;
     }
     h[i * kEpiThreads] = x;
@@ -165,9 +176,10 @@ __device__ __forceinline__ void heap_sift_down(float* h, int n, float x) {
 __device__ __forceinline__ void heap_push(float* h, int n, float x) {
     int i = n;
     while (i > 0) {
-        int pnt = (i - 1) >> 1;
-        if (h[pnt * kEpiThreads] >= x) break;
-        h[i * kEpiThreads] = h[pnt * kEpiThreads];
+        const int pnt = (i - 1) >> 2;
+        const float pv = h[pnt * kEpiThreads];
+        if (pv >= x) break;
+        h[i * kEpiThreads] = pv;
         i = pnt;
     }
     h[i * kEpiThreads] = x;

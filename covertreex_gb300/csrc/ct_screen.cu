@@ -991,6 +991,26 @@ __device__ __forceinline__ void df_combine(float& hi, float& lo, float oh, float
     hi = t;
     lo = __fadd_rn(__fadd_rn(lo, ol), err);
 }
+// The same two steps on two independent sums at once (f32x2; each component rounds as the
+// scalar __fadd_rn / __fmul_rn / __fmaf_rn do, and x - y is x + (-y) exactly), so either
+// component's bits equal the scalar routine's.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void two_sum_acc2(float2& s, float2& comp, float2 a, float2 b) {
+    const float2 pr = __fmul2_rn(a, b);
+    const float2 pe = __ffma2_rn(a, b, neg2(pr));
+    const float2 ts = __fadd2_rn(s, pr);
+    const float2 z = __fadd2_rn(ts, neg2(s));
+    const float2 se = __fadd2_rn(__fadd2_rn(s, neg2(__fadd2_rn(ts, neg2(z)))), __fadd2_rn(pr, neg2(z)));
+    s = ts;
+    comp = __fadd2_rn(comp, __fadd2_rn(se, pe));
+}
+__device__ __forceinline__ void df_combine2(float2& hi, float2& lo, float2 oh, float2 ol) {
+    const float2 t = __fadd2_rn(hi, oh);
+    const float2 z = __fadd2_rn(t, neg2(hi));
+    const float2 err = __fadd2_rn(__fadd2_rn(hi, neg2(__fadd2_rn(t, neg2(z)))), __fadd2_rn(oh, neg2(z)));
+    hi = t;
+    lo = __fadd2_rn(__fadd2_rn(lo, ol), err);
+}
 
 // Dots of the query slice with NC candidate rows at once (independent loads in flight).
 // Lane L sums elements [L m/32, (L+1) m/32) in order; the lanes' pairs are combined by a
@@ -1541,7 +1561,7 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
     extern __shared__ __align__(16) unsigned char xs_raw[];
     const int m = P.m, k = P.k;
     float* cs = (float*)xs_raw;                                            // [m][XC]
-    float* qs = cs + (size_t)m * XC;                                       // [XQ][m]
+    float* qs = cs + (size_t)m * XC;                                       // [XQ/2][m][2]
     unsigned long long* kb = (unsigned long long*)(qs + (size_t)XQ * m);  // [XQ][XKB]
     __shared__ int cid_s[XC];
     __shared__ int qid_s[XQ];
@@ -1551,10 +1571,11 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x < XQ) qid_s[threadIdx.x] = threadIdx.x < G.ng ? P.slot_id[P.full_slots[G.g0 + threadIdx.x]] : -1;
     __syncthreads();
+    // query rows interleaved by warp pair: element t of slots w and w + 8 side by side
     for (int e = threadIdx.x; e < XQ * m; e += blockDim.x) {
-        const int g = e / m;
+        const int g = e / m, t = e - g * m;
         const int q = qid_s[g];
-        qs[e] = q >= 0 ? P.v[(size_t)q * m + (e - g * m)] : 0.f;
+        qs[((size_t)(g & 7) * m + t) * 2 + (g >> 3)] = q >= 0 ? P.v[(size_t)q * m + t] : 0.f;
     }
     for (int e = threadIdx.x; e < XQ * XKB; e += blockDim.x) kb[e] = ~0ULL;
     long long c_lo = 0, total = 0;
@@ -1575,8 +1596,7 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
     const int ida = qid_s[ga], idb = qid_s[gb];
     unsigned long long* ka = kb + (size_t)ga * XKB;
     unsigned long long* kbb = kb + (size_t)gb * XKB;
-    const float* qa = qs + (size_t)ga * m;
-    const float* qb = qs + (size_t)gb * m;
+    const float* q2 = qs + (size_t)ga * m * 2;  // (slot ga, slot gb) pairs
     int fa = k, fb = k;
     long long evals = 0;
     __syncthreads();
@@ -1618,33 +1638,28 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
         // the butterfly does (lane offsets 16, 8, 4, 2, 1).  Taking segment rev5(c) at step
         // c turns that tree into a binary counter: pend[L] holds the finished subtree of
         // 2^L segments while bit L of c is set.
-        float ha = 0.f, la = 0.f, hb = 0.f, lb = 0.f;
-        float pend[5][4];
+        float2 h2 = make_float2(0.f, 0.f), l2 = make_float2(0.f, 0.f);  // (slot ga, slot gb)
+        float2 pend_h[5], pend_l[5];
 #pragma unroll
-        for (int L = 0; L < 5; ++L) pend[L][0] = pend[L][1] = pend[L][2] = pend[L][3] = 0.f;
+        for (int L = 0; L < 5; ++L) pend_h[L] = pend_l[L] = make_float2(0.f, 0.f);
         for (int c = 0; c < 32; ++c) {
             const int seg = (int)(__brev((unsigned)c) >> 27);
-            const float* qas = qa + seg * per;
-            const float* qbs = qb + seg * per;
+            const float* q2s = q2 + seg * per * 2;
             const float* css = cs + (size_t)seg * per * XC + lane;
-            ha = 0.f; la = 0.f; hb = 0.f; lb = 0.f;
+            h2 = make_float2(0.f, 0.f); l2 = make_float2(0.f, 0.f);
             if (PER > 0) {
 #pragma unroll
-                for (int t4 = 0; t4 < PER; t4 += 4) {
-                    const float4 a4 = *(const float4*)(qas + t4);
-                    const float4 b4 = *(const float4*)(qbs + t4);
+                for (int t4 = 0; t4 < PER; t4 += 2) {
+                    const float4 ab = *(const float4*)(q2s + 2 * t4);  // a[t4], b[t4], a[t4+1], b[t4+1]
                     const float x0 = css[(t4 + 0) * XC], x1 = css[(t4 + 1) * XC];
-                    const float x2 = css[(t4 + 2) * XC], x3 = css[(t4 + 3) * XC];
-                    two_sum_acc(ha, la, a4.x, x0); two_sum_acc(hb, lb, b4.x, x0);
-                    two_sum_acc(ha, la, a4.y, x1); two_sum_acc(hb, lb, b4.y, x1);
-                    two_sum_acc(ha, la, a4.z, x2); two_sum_acc(hb, lb, b4.z, x2);
-                    two_sum_acc(ha, la, a4.w, x3); two_sum_acc(hb, lb, b4.w, x3);
+                    two_sum_acc2(h2, l2, make_float2(ab.x, ab.y), make_float2(x0, x0));
+                    two_sum_acc2(h2, l2, make_float2(ab.z, ab.w), make_float2(x1, x1));
                 }
             } else {
                 for (int t = 0; t < per; ++t) {
                     const float x = css[t * XC];
-                    two_sum_acc(ha, la, qas[t], x);
-                    two_sum_acc(hb, lb, qbs[t], x);
+                    const float2 ab = *(const float2*)(q2s + 2 * t);
+                    two_sum_acc2(h2, l2, ab, make_float2(x, x));
                 }
             }
             bool placed = false;
@@ -1652,15 +1667,15 @@ __global__ void __launch_bounds__(256) rescore_tile_kernel(RescoreParams P, cons
             for (int L = 0; L < 5; ++L) {
                 if (!placed) {
                     if ((c >> L) & 1) {
-                        df_combine(ha, la, pend[L][0], pend[L][1]);
-                        df_combine(hb, lb, pend[L][2], pend[L][3]);
+                        df_combine2(h2, l2, pend_h[L], pend_l[L]);
                     } else {
-                        pend[L][0] = ha; pend[L][1] = la; pend[L][2] = hb; pend[L][3] = lb;
+                        pend_h[L] = h2; pend_l[L] = l2;
                         placed = true;
                     }
                 }
             }
         }
+        const float ha = h2.x, la = l2.x, hb = h2.y, lb = l2.y;
         const df da = df_fast(ha, la);
         const df db = df_fast(hb, lb);
         const float dista = va ? exact_from_dot(P, ida, cid, da) : 0.f;

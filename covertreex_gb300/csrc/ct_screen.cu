@@ -1923,11 +1923,13 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
             }
             asm volatile("cp.async.commit_group;\n" ::: "memory");
         };
-        float tot[QPT][4];
+        // running sums of queries (2i, 2i + 1) x candidate j as f32x2 (each component
+        // rounds as __fmaf_rn / __fadd_rn do)
+        float2 tot[QPT / 2][4];
 #pragma unroll
-        for (int i = 0; i < QPT; ++i)
+        for (int i = 0; i < QPT / 2; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) tot[i][j] = 0.f;
+            for (int j = 0; j < 4; ++j) tot[i][j] = make_float2(0.f, 0.f);
         stage(0, 0);
         for (int kc = 0; kc < nk; ++kc) {
             if (kc + 1 < nk) {
@@ -1941,11 +1943,11 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
             const float* qb = qsT + (size_t)kc * FKC * FQP + QPT * tq;
 #pragma unroll
             for (int h = 0; h < FKC / FLB; ++h) {
-                float acc[QPT][4];
+                float2 acc[QPT / 2][4];
 #pragma unroll
-                for (int i = 0; i < QPT; ++i)
+                for (int i = 0; i < QPT / 2; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+                    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
 #pragma unroll
                 for (int k4 = 0; k4 < FLB; k4 += 4) {
                     const int kk = h * FLB + k4;
@@ -1954,31 +1956,35 @@ __global__ void __launch_bounds__(256, 1) filter_tile_kernel(RescoreParams P, co
                     for (int j = 0; j < 4; ++j) x[j] = *(const float4*)(cb + (tc + 64 * j) * FKP + kk);
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {
-                        float qv[QPT];
+                        float2 qv[QPT / 2];
 #pragma unroll
                         for (int i4 = 0; i4 < QPT; i4 += 4) {
                             const float4 qa = *(const float4*)(qb + (kk + t) * FQP + i4);
-                            qv[i4] = qa.x; qv[i4 + 1] = qa.y; qv[i4 + 2] = qa.z; qv[i4 + 3] = qa.w;
+                            qv[i4 / 2] = make_float2(qa.x, qa.y); qv[i4 / 2 + 1] = make_float2(qa.z, qa.w);
                         }
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             const float xv = t == 0 ? x[j].x : t == 1 ? x[j].y : t == 2 ? x[j].z : x[j].w;
+                            const float2 x2 = make_float2(xv, xv);
 #pragma unroll
-                            for (int i = 0; i < QPT; ++i) acc[i][j] = __fmaf_rn(qv[i], xv, acc[i][j]);
+                            for (int i = 0; i < QPT / 2; ++i) acc[i][j] = __ffma2_rn(qv[i], x2, acc[i][j]);
                         }
                     }
                 }
 #pragma unroll
-                for (int i = 0; i < QPT; ++i)
+                for (int i = 0; i < QPT / 2; ++i)
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) tot[i][j] = __fadd_rn(tot[i][j], acc[i][j]);
+                    for (int j = 0; j < 4; ++j) tot[i][j] = __fadd2_rn(tot[i][j], acc[i][j]);
             }
             __syncthreads();  // buffer kc & 1 is free for chunk kc + 2 (and, at the end, for the dots)
         }
 #pragma unroll
-        for (int i = 0; i < QPT; ++i)
+        for (int i = 0; i < QPT / 2; ++i)
 #pragma unroll
-            for (int j = 0; j < 4; ++j) dots[(QPT * tq + i) * FDP + tc + 64 * j] = tot[i][j];
+            for (int j = 0; j < 4; ++j) {
+                dots[(QPT * tq + 2 * i) * FDP + tc + 64 * j] = tot[i][j].x;
+                dots[(QPT * tq + 2 * i + 1) * FDP + tc + 64 * j] = tot[i][j].y;
+            }
         __syncthreads();
         // F bounds and E, warp w owns query rows w, w + 8, ...
         for (int r = 0; r < RPW; ++r) {

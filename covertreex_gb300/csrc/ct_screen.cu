@@ -189,9 +189,8 @@ __device__ __forceinline__ void heap_push(float* h, int n, float x) {
 __device__ __forceinline__ bool jb_warm_seen(const Job& jb) { return (jb.which & 4) != 0; }
 
 // Squared scaled distance and kernel value of one query with two staged candidates
-// (columns .x and .y of the record pair r4), every operation explicitly rounded so that
-// the epilogue's tiers see the same bits for a pair.  Matern also returns a = sqrt(5 d2)
-// and e^-a for the error term.
+// (columns .x and .y of the record pair r4).  Matern also returns a = sqrt(5 d2) and e^-a
+// for the error term.
 template <int DP, int KT>
 __device__ __forceinline__ void pair_kv2(const float4* r4, const float (&nxq)[kMaxD], float var, float2& d2,
                                          float2& kv, float2& a, float2& ea) {
@@ -555,11 +554,13 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                     for (int i = 0; i < 8; ++i) rmax = fmaxf(rmax, fmaxf(kmax - v[i], v[i]));
                     const float ghi = (rmax * (1.f + 3e-7f) + vnq * gr[0] + ekmax + 1e-30f) * gr[1] * (1.f + 1e-6f);
                     if (!(ghi >= thr_keep)) continue;
-                    // Second tier: each pair's kernel value, computed exactly as phase 1 does,
-                    // gives phase 1's R = |kv - s| bit for bit; with the group's largest error
-                    // term and 1/sqrt(p) as above, rc bounds phase 1's survivor bound of every
-                    // pair.  Near candidates pass the box test (the box cannot see that s
-                    // tracks kv) but rarely this one; it costs about half of phase 1.
+                    // Second tier: each pair's kernel value, computed as phase 1 does, gives
+                    // phase 1's R = |kv - s| up to the product kv being fused into the add in
+                    // one tier and not the other (which moves kv - s by at most 2^-23 kv); with
+                    // 2.4e-7 kv added, and the group's largest error term and 1/sqrt(p) as
+                    // above, rc bounds phase 1's survivor bound of every pair.  Near
+                    // candidates pass the box test (the box cannot see that s tracks kv) but
+                    // rarely this one; it costs about half of phase 1.
                     float rc = 0.f;
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
@@ -567,7 +568,9 @@ __global__ void __launch_bounds__(kThreads, 1) screen_sweep_kernel(MMAParams P) 
                         float2 d2, kv, am, ea;
                         pair_kv2<DP, KT>(r4, nxq, P.var, d2, kv, am, ea);
                         const float2 dif = __fadd2_rn(kv, make_float2(-v[2 * i], -v[2 * i + 1]));
-                        rc = fmaxf(rc, fmaxf(fabsf(dif.x), fabsf(dif.y)));
+                        const float2 rr = __ffma2_rn(kv, make_float2(2.4e-7f, 2.4e-7f),
+                                                     make_float2(fabsf(dif.x), fabsf(dif.y)));
+                        rc = fmaxf(rc, fmaxf(rr.x, rr.y));
                     }
                     const float gc = (rc * (1.f + 3e-7f) + vnq * gr[0] + ekmax + 1e-30f) * gr[1] * (1.f + 1e-6f);
                     if (!(gc >= thr_keep)) continue;
@@ -992,8 +995,11 @@ __device__ __forceinline__ void df_combine(float& hi, float& lo, float oh, float
     lo = __fadd_rn(__fadd_rn(lo, ol), err);
 }
 // The same two steps on two independent sums at once (f32x2; each component rounds as the
-// scalar __fadd_rn / __fmul_rn / __fmaf_rn do, and x - y is x + (-y) exactly), so either
-// component's bits equal the scalar routine's.
+// scalar __fadd_rn / __fmul_rn / __fmaf_rn do, and x - y is x + (-y) exactly).  Measured
+// on GB300: an f32x2 multiply whose only use is an f32x2 add gives the bits of a fused
+// multiply-add in about 5% of random cases, with or without -fmad=false; here the product
+// pr has several uses, and the forced exhaustive tests check that these passes and the
+// scalar warp reduction agree bit for bit.
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ void two_sum_acc2(float2& s, float2& comp, float2 a, float2 b) {
     const float2 pr = __fmul2_rn(a, b);

@@ -320,3 +320,114 @@ def test_group_test_bounds_every_pair(n, d, m, kt, ls):
                     if q in cands:  # the group holding the query can never be rejected
                         isq = data[3][q]
                         assert float(g) >= (1.0 - 2e-6) / float(isq)
+
+
+def _kv_variants(q, c, data, pick):
+    """The kernel value of pair_kv2 (screen_sweep_kernel) for one pair, float32 operation by
+    operation, in every form the compiler may produce: each entry is (kv, exact product
+    whose rounding is kv, d2, a, e^-a), with the Matern polynomial's a^2/3 term fused into
+    its add or not."""
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    d2 = F(0.0)
+    for a_ in range(d):
+        t = F(xs[c, a_] + F(-xs[q, a_]))
+        d2 = fma32(t, t, d2)
+    if kt == 0:
+        e = expf_band(F(F(-0.5) * d2))[pick]
+        return [(F(F(var) * e), np.float64(var) * np.float64(e), d2, F(0.0), F(0.0))]
+    a = F(F(2.2360679775) * F(np.sqrt(d2)))
+    ea = expf_band(F(-a))[pick]
+    out = []
+    for fuse_poly in (False, True):
+        a2 = F(a * a)
+        one_a = F(F(1.0) + a)
+        poly = F(np.float64(a2) * np.float64(F(0.33333334)) + np.float64(one_a)) if fuse_poly \
+            else F(one_a + F(a2 * F(0.33333334)))
+        vp = F(F(var) * poly)
+        out.append((F(vp * ea), np.float64(vp) * np.float64(ea), d2, a, ea))
+    return out
+
+
+def _dif_variants(kv, prod, v):
+    """kv - s with the product kept (rounded kv) or fused into the add (one rounding)."""
+    return [F(kv + F(-v)), F(prod - np.float64(v))]
+
+
+def _phase1_bhi(q, c, data, kv, dif, d2, a, ea):
+    Vf, xs, vn, isp, xmax, xmax_max, var, kt, m, d = data
+    u2 = 1.0 / 65536.0
+    err_coef = F(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22)
+    err_c = F(err_coef * vn[c])
+    dd = F(d)
+    ced2 = F(F(dd + F(2.0)) * F(5.97e-8))
+    A = F(F(2.4e-7) * F(xmax[q] + xmax_max))
+    ale = F(F(ced2 + F(F(F(0.5) * A) * dd)) * F(1.00001))
+    bee = F(F(F(0.5) * A) * F(1.00001))
+    alk = F(F(F(F(6e-8) + F(F(0.5) * ced2)) + F(F(F(0.25) * A) * dd)) * F(1.00001))
+    bek = F(F(F(1e-6) + F(F(0.25) * A)) * F(1.00001))
+    if kt == 0:
+        ek = F(kv * fma32(alk, d2, bek))
+    else:
+        ed2 = fma32(ale, d2, bee)
+        t1 = F(kv * F(F(1e-6) + F(F(2.4e-7) * a)))
+        t2 = F(F(F(F(var) * F(F(F(0.8334) * ed2) + F(F(F(1e-7) * a) * a))) * F(F(1.0) + a)) * ea)
+        ek = F(t1 + t2)
+    R = F(abs(dif))
+    e = F(fma32(vn[q], err_c, ek) + fma32(R, F(1.2e-7), F(1e-30)))
+    return F(F(R + e) * isp[c])
+
+
+@pytest.mark.parametrize("n,d,m,kt,ls", [
+    (1500, 8, 64, 0, 2.0),   # RBF, precision-workload-like
+    (1500, 3, 64, 1, 1.0),   # Matern 5/2
+    (1200, 3, 128, 0, 0.7),  # RBF, short lengthscale
+    (1200, 5, 96, 1, 2.0),   # Matern, D = 5
+])
+def test_second_tier_bounds_every_pair(n, d, m, kt, ls):
+    """The sweep's second group tier (per-pair kernel values, screen_sweep_kernel) never
+    rejects a group holding a pair that phase 1 would keep or heap: with 2.4e-7 kv added to
+    each |kv - s|, its bound is >= phase 1's survivor bound bhi of every pair, whichever of
+    the two tiers has the kernel value's last multiply (and the Matern polynomial's) fused
+    into the following add, for tensor-core dots anywhere in the certified band and __expf
+    at either end of its band; groups of near points (where the tier decides), random groups
+    and groups with tiny-p rows."""
+    X, V, p, idx, data = _case(n, d, m, kt, ls, seed=n + d + m + 7)
+    xs, vn, isp = data[1], data[2], data[3]
+    u2 = 1.0 / 65536.0
+    err_coef = F(3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22)
+    c_split = 3.1 * u2 + (3.0 * m / 16.0 + 17.0) * 2.0 ** -22
+    r = np.random.default_rng(29)
+    order = np.lexsort(tuple(xs[:, a] for a in range(d)))
+    groups = [order[s:s + 8] for s in r.choice(n - 8, 8, replace=False)]
+    groups += [r.choice(n, 8, replace=False) for _ in range(3)]
+    groups += [np.concatenate([idx[:2], r.choice(n, 6, replace=False)])]
+    queries = [int(g[3]) for g in groups[:5]] + [int(idx[0])]  # members of near groups, an inducing row
+    checked = 0
+    for q in queries:
+        ekmax = _query_consts(q, data)
+        for g in groups:
+            cands = [int(c) for c in g if int(c) != q]
+            err_max = max(F(err_coef * vn[c]) for c in cands)
+            isc_max = max(isp[c] for c in cands)
+            for shift in (-1.0, 0.0, 1.0):
+                vs = {c: F(float(np.dot(V[q].astype(np.float64), V[c].astype(np.float64)))
+                           + shift * c_split * float(vn[q]) * float(vn[c])) for c in cands}
+                for pick in (0, 1, 2):
+                    kvs = {c: _kv_variants(q, c, data, pick) for c in cands}
+                    # tier 2 in each compiled form (the same form for every pair of the group)
+                    n_forms = len(kvs[cands[0]]) * 2
+                    for form in range(n_forms):
+                        rc = F(0.0)
+                        for c in cands:
+                            kv, prod, _, _, _ = kvs[c][form // 2]
+                            dif = _dif_variants(kv, prod, vs[c])[form % 2]
+                            rc = max(rc, fma32(kv, F(2.4e-7), F(abs(dif))))
+                        inner = F(F(F(rc * F(1.0 + 3e-7)) + F(vn[q] * err_max)) + F(ekmax + F(1e-30)))
+                        gc = F(F(inner * isc_max) * F(1.0 + 1e-6))
+                        for c in cands:
+                            for kv, prod, d2, a, ea in kvs[c]:
+                                for dif in _dif_variants(kv, prod, vs[c]):
+                                    bhi = _phase1_bhi(q, c, data, kv, dif, d2, a, ea)
+                                    assert gc >= bhi, (q, c, form, pick, float(gc), float(bhi))
+                                    checked += 1
+    assert checked > 1000

@@ -451,7 +451,7 @@ def bench_serving(dev, rates, seconds: float):
     5/2, m=256; 90% queries of 1..4096 new points, k in {30,50,60}) served with
     continuous batching against a 120 GB HBM budget, beside the plain per-request form."""
     from covertreex_gb300 import _lib, synthetic
-    from covertreex_gb300.serving import QueryRequest, ServingEngine, latency_summary
+    from covertreex_gb300.serving import QueryRequest, ServingEngine, latency_by_size, latency_summary
 
     # Library phase timing off on this thread (it is per thread): with it on, every dense
     # step's ct_batch_run waits for its kernel to read the elapsed time, which serialises the
@@ -473,6 +473,7 @@ def bench_serving(dev, rates, seconds: float):
             wall = time.perf_counter() - t0
             row = {"rate_req_s": rate, "requests": len(stream), "wall_s": wall,
                    "query": latency_summary(recs, "query"), "build": latency_summary(recs, "build"),
+                   "query_by_points": latency_by_size(recs, "query"),
                    "peak_hbm_GB": eng.peak_bytes / 1e9, "evicted": len(eng.evicted),
                    "gpu_launches": eng.launches - l0}
         finally:

@@ -556,5 +556,20 @@ def latency_summary(records: List[RequestRecord], kind: str = "query") -> dict:
             "forms": {f: sum(1 for r in ok if r.form == f) for f in ("dense", "screened")}}
 
 
+def latency_by_size(records: List[RequestRecord], kind: str = "query",
+                    edges=(1, 16, 256, 1024, 4097)) -> List[dict]:
+    """p50 / p99 / max latency of the finished requests of one kind per size bucket
+    [edges[i], edges[i+1]) (query points, or build rows); empty buckets are left out."""
+    out = []
+    ok = [r for r in records if r.kind == kind and r.status == "ok"]
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        lat = np.array([r.latency_ms for r in ok if lo <= r.size < hi])
+        if lat.size == 0:
+            continue
+        out.append({"size": f"{lo}-{hi - 1}", "count": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
+                    "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max())})
+    return out
+
+
 __all__ = ["BuildRequest", "QueryRequest", "RequestRecord", "ServingEngine", "estimate_tree_bytes",
-           "latency_summary"]
+           "latency_by_size", "latency_summary"]

@@ -95,6 +95,19 @@ def test_serving_estimates_and_summary():
     assert abs(s["p50_ms"] - 2.0) < 1e-6 and abs(s["p99_ms"] - 2.0) < 1e-6
 
 
+def test_serving_latency_by_size():
+    from covertreex_gb300.serving import RequestRecord, latency_by_size
+
+    recs = [RequestRecord(rid=i, kind="query", arrival=0.0, size=size, done=ms / 1e3, status="ok", form="dense")
+            for i, (size, ms) in enumerate([(1, 1.0), (8, 2.0), (300, 5.0), (4096, 9.0), (2000, 7.0)])]
+    recs.append(RequestRecord(rid=9, kind="query", arrival=0.0, size=20, status="evicted"))
+    recs.append(RequestRecord(rid=10, kind="build", arrival=0.0, size=5000, done=0.5, status="ok"))
+    b = latency_by_size(recs)
+    assert [x["size"] for x in b] == ["1-15", "256-1023", "1024-4096"]  # the evicted 20-point request is not counted
+    assert [x["count"] for x in b] == [2, 1, 2]
+    assert abs(b[0]["max_ms"] - 2.0) < 1e-9 and abs(b[2]["p50_ms"] - 8.0) < 1e-9 and abs(b[2]["max_ms"] - 9.0) < 1e-9
+
+
 def test_runtime_api_host_checks():
     import pytest as _pytest
 
